@@ -1,0 +1,276 @@
+"""Benchmark: MLUPS and HBM roofline fraction of the stream+collide step.
+
+Workload (default): the D3Q19 MRT periodic Taylor-Green vortex on 256^3
+nodes, populations stored in FP32 as deviations from the rest equilibrium,
+FP32 arithmetic.  One step = one fused pull-stream + collide launch over all
+16.8 M nodes (the domain is periodic along every axis, so there is no ghost
+refresh or boundary kernel).  Each buffer is 1.3 GB, ten times the L2, so
+every step streams from HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference algorithm (the
+C oracle, all host cores, OpenMP) on a bounded sample of the same workload.
+With N > 1 (torchrun) every rank runs an independent replica (the path has
+no cross-GPU exchange); value = total nodes updated by all ranks / max time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_VALUE = {"float64": 8, "float32": 4, "float16": 2, "bfloat16": 2}
+DTYPE_TAG = {"float64": "f64", "float32": "f32", "float16": "f16", "bfloat16": "bf16"}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(args, steps, sample_grid):
+    """The C oracle (reference algorithm restated, float64, all cores) on a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import OracleSimulation
+    from pylbm_gb300 import workloads as W
+
+    cores = os.cpu_count() or 1
+    o = OracleSimulation(W.tgv3d(n=sample_grid), nthreads=cores)
+    o.initialize()
+    o.one_time_step()  # warm-up
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    mlups = sample_grid ** 3 * steps / dt / 1e6
+    return {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"D3Q19 TGV {sample_grid}^3, {steps} steps, float64, C oracle with OpenMP over {cores} threads"}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    base = cpu_reference(args, steps=max(args.steps // 10, 2), sample_grid=args.cpu_grid)
+    line = {"impl": "reference", "metric": "MLUPS", "value": base["value"], "unit": "MLUPS", "n_gpus": world,
+            "steps": max(args.steps // 10, 2), "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "D3Q19 MRT periodic Taylor-Green vortex (sample of the 256^3 grid)",
+                       "grid": [args.cpu_grid] * 3},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="grid size per axis")
+    ap.add_argument("--dtype", default="float32", choices=list(BYTES_PER_VALUE))
+    ap.add_argument("--cpu-grid", type=int, default=128)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    from pylbm_gb300 import Simulation, runtime
+    from pylbm_gb300 import workloads as W
+
+    runtime.check(runtime.core().lbm_set_device(local))
+    n = args.n
+    nodes = n ** 3
+    sim = Simulation(W.tgv3d(n=n), dtype=args.dtype)
+    assert sim.periodic
+    for _ in range(args.warmup):
+        sim.one_time_step()
+    sim.synchronize()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = runtime.Event(), runtime.Event()
+    e0.record(sim._stream)
+    for _ in range(args.steps):
+        sim.one_time_step()
+    e1.record(sim._stream)
+    ms = e0.elapsed_ms(e1)
+    clocks = sampler.stop()
+    sim.synchronize()
+    times = [ms]
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        times = [float(t.item())]
+    ms_total = times[0]
+    ms_step = ms_total / args.steps
+    value = nodes * args.steps * world / (ms_total / 1e3) / 1e6
+    bpl = 2 * sim.scheme.nv * BYTES_PER_VALUE[args.dtype]
+    achieved = bpl * nodes / (ms_step / 1e3) / 1e9
+    peak, peak_src = measured_peaks()
+    traffic = profiled_traffic(f"ncu_step_tgv3d_{DTYPE_TAG[args.dtype]}.txt") if n == 256 else None
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = end_to_end(sim, args, nodes)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_reference(args, steps=3, sample_grid=args.cpu_grid)
+
+    # check the result is sane (mass conserved, finite)
+    sums, bad = sim.population_sums()
+    if bad:
+        raise FloatingPointError("non-finite populations after the timed steps")
+
+    if rank == 0:
+        line = {
+            "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": DTYPE_TAG[args.dtype], "data": "synthetic",
+            "config": {"workload": f"D3Q19 MRT periodic Taylor-Green vortex {n}^3, {args.dtype} shifted storage, "
+                                   f"{'f64' if args.dtype == 'float64' else 'f32'} arithmetic",
+                       "grid": [n, n, n], "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (%.2f GB per population buffer)" % (sim._F.nbytes / 1e9)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_src, "bytes_per_lup": bpl,
+                         "kernel": "lbm_scheme::k_step_periodic"},
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+        }
+        if e2e:
+            line["e2e"] = e2e
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def end_to_end(sim, args, nodes):
+    """Same metric through the public API with host buffers.
+
+    Timed: upload of the initial populations from pinned host memory, K
+    calls of Simulation.one_time_step(), download of the conserved moments
+    (rho, qx, qy, qz) of the final state -- copies inside the timed region.
+    """
+    from pylbm_gb300 import runtime
+
+    es = BYTES_PER_VALUE[args.dtype]
+    nbytes = sim._F.nbytes
+    pinned = runtime.PinnedBuffer(nbytes)
+    runtime.check(runtime.core().lbm_memcpy(ctypes.c_void_p(pinned.ptr), sim._F.handle, nbytes, runtime.D2H, None))
+    out = runtime.PinnedBuffer(8 * sim._mlat.vstride * sim.scheme.nconsm)
+    sim.synchronize()
+    t0 = time.perf_counter()
+    runtime.check(runtime.core().lbm_memcpy(sim._F.handle, ctypes.c_void_p(pinned.ptr), nbytes, runtime.H2D, None))
+    for _ in range(args.steps):
+        sim.one_time_step()
+    sim.module.call(sim.module.lib.lbm_f2m(sim._F.handle, ctypes.byref(sim._lat), sim._mbuf().handle,
+                                           ctypes.byref(sim._mlat), None))
+    d2h = 8 * sim._mlat.vstride * sim.scheme.nconsm
+    runtime.check(runtime.core().lbm_memcpy(ctypes.c_void_p(out.ptr), sim._mbuf().handle, d2h, runtime.D2H, None))
+    sim.synchronize()
+    dt = time.perf_counter() - t0
+    return {"value": nodes * args.steps / dt / 1e6, "unit": "MLUPS",
+            "h2d_bytes_per_step": nbytes / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+            "note": f"pinned H2D of the initial state, {args.steps} API steps, D2H of the conserved moments"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,193 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300 stream+collide backend for pylbm.
+ *
+ * Two shared libraries export this ABI:
+ *
+ *   liblbm_gb300.so      scheme-independent runtime: device memory, streams,
+ *                        the periodic ghost refresh, the boundary-node kernels
+ *                        and the FP64 conservation sums.
+ *   lbm_scheme_<id>.so   one per scheme and storage type, generated and
+ *                        compiled from the scheme's sympy description (as
+ *                        pylbm compiles one Cython module per scheme), holding
+ *                        the fused pull-stream + collide and the moment
+ *                        transforms.
+ *
+ * Conventions: every entry point returns LBM_OK (0) or an error code and never
+ * throws or aborts; lbm_last_error() / lbm_scheme_last_error() give the message
+ * of the last failure of the calling thread.  Pointers named f, fnew, m, rhs,
+ * istore, iload0 and sums are DEVICE pointers; lbm_lattice and prm are HOST
+ * pointers read during the call.  `stream` is a cudaStream_t (NULL = legacy
+ * default stream).  Calls only enqueue work unless stated otherwise.
+ *
+ * Population storage: structure of arrays, one array per population, each a
+ * halo-extended box with the last axis contiguous (pylbm's index order
+ * f[k, ix, iy, iz], pylbm/storage.py:423 SOA).  Element (k, i0, i1, i2) in
+ * halo coordinates lives at
+ *     k*vstride + origin + i0*stride[0] + i1*stride[1] + i2*stride[2]
+ * where the stride of the last axis is 1 and rows of the last axis are padded
+ * so that interior rows start on 32-byte boundaries (lbm_lattice_init).
+ * With shifted storage the stored value is f_k - shift[k].
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_MAX_Q 64
+
+enum lbm_status {
+  LBM_OK = 0,
+  LBM_ERR_ARG = 1,         /* invalid argument (sizes, types, null pointers) */
+  LBM_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  LBM_ERR_NONFINITE = 3,   /* a NaN or Inf was found in the populations */
+  LBM_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  LBM_ERR_UNSUPPORTED = 5  /* configuration not handled by this build */
+};
+
+enum lbm_dtype { LBM_F64 = 0, LBM_F32 = 1, LBM_F16 = 2, LBM_BF16 = 3 };
+
+enum lbm_copy_kind { LBM_H2D = 0, LBM_D2H = 1, LBM_D2D = 2 };
+
+typedef struct lbm_lattice {
+  int32_t dim;                /* 1, 2 or 3 */
+  int32_t nv;                 /* number of populations */
+  int32_t dtype;              /* enum lbm_dtype of the stored values */
+  int32_t reserved;
+  int32_t n[3];               /* interior nodes per axis (1 beyond dim) */
+  int32_t halo[3];            /* ghost layers per axis (0 beyond dim) */
+  int64_t stride[3];          /* element stride per axis; stride[dim-1] == 1 */
+  int64_t vstride;            /* element stride between populations */
+  int64_t origin;             /* element offset of halo index (0,0,0) */
+  int64_t elements;           /* total elements of the allocation (nv*vstride) */
+  double shift[LBM_MAX_Q];    /* stored value = f_k - shift[k] */
+} lbm_lattice;
+
+/* ------------------------------------------------------------------ */
+/* liblbm_gb300.so: runtime                                             */
+/* ------------------------------------------------------------------ */
+
+const char* lbm_version(void);
+const char* lbm_last_error(void);
+
+/* Fill the strides of the padded structure-of-arrays layout described
+ * above for `dim` axes of n[d] interior nodes and halo[d] ghost layers;
+ * shift[] is zeroed.  Host-only. */
+int lbm_lattice_init(lbm_lattice* lat, int32_t dim, int32_t nv, int32_t dtype,
+                     const int32_t* n, const int32_t* halo);
+
+int lbm_device_count(int32_t* count);
+int lbm_set_device(int32_t device);
+int lbm_device_synchronize(void);
+
+/* Device memory and copies (replace the pyopencl arrays of pylbm's LOOPY
+ * containers, pylbm/storage.py:109-157, pylbm/boundary.py:378-397). */
+int lbm_alloc(void** ptr, size_t bytes);
+int lbm_free(void* ptr);
+int lbm_memcpy(void* dst, const void* src, size_t bytes, int32_t kind, void* stream);
+int lbm_memset(void* ptr, int32_t value, size_t bytes, void* stream);
+int lbm_stream_create(void** stream);
+int lbm_stream_destroy(void* stream);
+int lbm_stream_synchronize(void* stream);
+
+/* Pinned host memory (for host<->device copies that overlap compute). */
+int lbm_host_alloc(void** ptr, size_t bytes);
+int lbm_host_free(void* ptr);
+
+/* CUDA events on a stream, for device-side timing. */
+int lbm_event_create(void** event);
+int lbm_event_destroy(void* event);
+int lbm_event_record(void* event, void* stream);
+int lbm_event_elapsed_ms(void* start, void* end, float* ms); /* synchronizes on `end` */
+
+/* Periodic ghost refresh of every axis: ghost layer i of an axis receives
+ * interior layer i +/- n (pylbm/storage.py:307-367 Array.update, a periodic
+ * halo exchange with itself on one process; LOOPY kernels update_x/y/z
+ * :370-420).  Boundary kernels run afterwards and overwrite the ghost
+ * populations they own, as in Simulation.boundary_condition
+ * (pylbm/simulation.py:374-390). */
+int lbm_update_halo(void* f, const lbm_lattice* lat, void* stream);
+
+/* Boundary-node kernels.  istore and iload0 are int32 arrays of shape
+ * (ncond, dim+1): velocity index then halo coordinates, the layout pylbm
+ * gives them after BoundaryMethod.fix_iload (pylbm/boundary.py:226-235).
+ * rhs is float64 (ncond).  Values are physical (shift applied inside).
+ *   bounce_back:       f[istore] =  f[iload0] + rhs   (pylbm/boundary.py:430-464)
+ *   anti_bounce_back:  f[istore] = -f[iload0] + rhs   (pylbm/boundary.py:646-680)
+ *   neumann:           f[istore] =  f[iload0]         (pylbm/boundary.py:787-818,
+ *                      also neumannx/y/z, which differ only in iload0)
+ * The links of one call must not read a population another link of the
+ * same call writes (true for lists built by pylbm's Boundary); `ordered`=1
+ * processes the links one after the other instead. */
+int lbm_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
+                    const double* rhs, const lbm_lattice* lat, int32_t ordered, void* stream);
+int lbm_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
+                         const double* rhs, const lbm_lattice* lat, int32_t ordered, void* stream);
+int lbm_neumann(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
+                const lbm_lattice* lat, int32_t ordered, void* stream);
+
+/* FP64 sums over the interior nodes of every population (physical values),
+ * the conservation diagnostic of the build (mass/momentum = M . sums).
+ * `partials` is caller-provided device scratch of at least
+ * lbm_population_sums_scratch_bytes() bytes.  sums (nv doubles) and
+ * nonfinite (one int32, set to the number of blocks that saw a NaN/Inf) are
+ * device pointers.  No reference counterpart: pylbm has no such check. */
+int lbm_population_sums_scratch_bytes(const lbm_lattice* lat, size_t* bytes);
+int lbm_population_sums(const void* f, const lbm_lattice* lat, double* sums, int32_t* nonfinite,
+                        void* partials, size_t partials_bytes, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* lbm_scheme_<id>.so: per-scheme module (generated constants + the     */
+/* kernel templates of pylbm_gb300/csrc/scheme_kernels.cuh)            */
+/* ------------------------------------------------------------------ */
+
+const char* lbm_scheme_last_error(void);
+
+/* Number of populations, dimension, number of run-time parameters,
+ * storage and compute types, and shift/mref (nv doubles each: the stored
+ * shift feq(c0) and its moments). */
+int lbm_scheme_describe(int32_t* nv, int32_t* dim, int32_t* nprm, int32_t* storage,
+                        int32_t* compute, double* shift, double* mref);
+
+/* One LBM step on the interior nodes: pull f_k(x - v_k), m = M f, relax
+ * the non-conserved moments toward m_eq(conserved) at rates s, fnew = M^-1 m
+ * (pylbm/algorithm/pull.py:11-59, pylbm/algorithm/base.py:551-600; generated
+ * routine `one_time_step(f, fnew, nx, ny[, nz])`).  prm holds the run-time
+ * parameters (free symbols of the scheme, sorted by name).  f must have its
+ * ghost layers filled (lbm_update_halo + boundary kernels). */
+int lbm_one_time_step(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                      void* stream);
+
+/* Same step for domains periodic along every axis: the pull wraps inside the
+ * interior, ghost layers are neither read nor written (no halo pass). */
+int lbm_one_time_step_periodic(const void* f, void* fnew, const lbm_lattice* lat,
+                               const double* prm, void* stream);
+
+/* Pure pull streaming on the interior (pylbm/algorithm/base.py:289-296). */
+int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* stream);
+
+/* Moments of every node, halo included: m = M f (pylbm/algorithm/base.py:
+ * 336-344).  m is float64 in its own lattice layout `mlat` (same n/halo). */
+int lbm_f2m(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat,
+            void* stream);
+
+/* Populations from moments: f = M^-1 m (pylbm/algorithm/base.py:346-379). */
+int lbm_m2f(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat,
+            void* stream);
+
+/* Non-conserved moments set to their equilibrium (pylbm/algorithm/base.py:
+ * 381-402); conserved moments are inputs. */
+int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void* stream);
+
+/* Moment-space relaxation m <- m + s (m_eq - m) (pylbm/algorithm/base.py:404-437). */
+int lbm_relaxation(double* m, const lbm_lattice* mlat, const double* prm, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

@@ -1,0 +1,202 @@
+"""Python driver of the C oracle (oracle/lbm_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of bench.py to check and time the GPU path.  The
+pylbm_gb300 package never imports it.
+
+``OracleSimulation`` replays pylbm's time step on the CPU in float64 with the
+reference's own order of operations (pylbm/simulation.py:374-420):
+periodic ghost exchange of every axis, boundary methods in list order, pull
+step on the interior, swap.  Scheme constants, domain and boundary lists come
+from pylbm_gb300's host code, which the golden fixtures pin against the
+reference separately.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import sympy as sp
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liblbm_oracle.so")
+SRC = os.path.join(HERE, "lbm_oracle.c")
+
+
+def build(force=False):
+    """Compile the oracle with gcc (OpenMP) into oracle/_build/."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp"
+    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-o", tmp, SRC, "-lm"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P, I = ctypes.c_void_p, ctypes.c_int
+        L.oracle_update_halo.argtypes = [P, I, I, P, P]
+        L.oracle_boundary.argtypes = [P, I, I, P, P, P, P, I, P, ctypes.c_double]
+        L.oracle_one_time_step.argtypes = [P, P, I, I, I, P, P, P, P, P, P, I, P, P, P, I]
+        L.oracle_f2m.argtypes = [P, P, I, I, P, P, P]
+        L.oracle_m2f.argtypes = [P, P, I, I, P, P, P]
+        L.oracle_equilibrium.argtypes = [P, I, I, I, P, P, I, P, P, P]
+        for fn in ("oracle_update_halo", "oracle_boundary", "oracle_one_time_step", "oracle_f2m", "oracle_m2f",
+                   "oracle_equilibrium"):
+            getattr(L, fn).restype = None
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def equilibrium_table(scheme, params=None):
+    """Monomial table (rows, coefs, exponents) of the scheme's equilibria."""
+    params = {str(k): v for k, v in (params or {}).items()}
+    cons = list(scheme.consm.keys())
+    rows, coefs, expos = [], [], []
+    for k in range(scheme.nconsm, scheme.nv):
+        e = scheme.EQ[k]
+        e = e.subs({s: params[str(s)] for s in e.free_symbols if str(s) in params})
+        e = sp.expand(e)
+        for term in sp.Add.make_args(e):
+            if term == 0:
+                continue
+            coef, facs = term.as_coeff_mul()
+            ex = [0] * len(cons)
+            c = float(coef)
+            for fac in facs:
+                base, p = fac.as_base_exp()
+                if base in cons and p.is_Integer:
+                    ex[cons.index(base)] += int(p)
+                elif not fac.free_symbols:
+                    c *= float(fac)
+                else:
+                    raise ValueError(f"equilibrium term {term} is not a monomial of the conserved moments")
+            rows.append(k)
+            coefs.append(c)
+            expos.append(ex)
+    return (np.array(rows, dtype=np.int32), np.array(coefs, dtype=np.float64),
+            np.ascontiguousarray(np.array(expos, dtype=np.int32).reshape(len(rows), len(cons))))
+
+
+class OracleSimulation:
+    """CPU float64 replay of a pylbm simulation (same dictionary)."""
+
+    def __init__(self, dico, nthreads=1):
+        from pylbm_gb300.boundary import Boundary
+        from pylbm_gb300.domain import Domain
+        from pylbm_gb300.scheme import Scheme
+
+        self.scheme = Scheme(dico)
+        self.domain = Domain(dico, self.scheme.stencil)
+        self.dim = self.domain.dim
+        self.nthreads = int(nthreads)
+        self.extra_parameters = {}
+        self.n = np.array(self.domain.shape_in, dtype=np.int32)
+        self.h = np.array(self.domain.halo, dtype=np.int32)
+        sc = self.scheme
+        v = np.zeros((sc.nv, 3), dtype=np.int32)
+        v[:, :self.dim] = sc.stencil.get_all_velocities()
+        self.vel = v
+        self.M = np.ascontiguousarray(sc.M)
+        self.invM = np.ascontiguousarray(sc.invM)
+        shape = [sc.nv] + self.domain.shape_halo
+        self.f = np.zeros(shape)
+        self.fnew = np.zeros(shape)
+        self.dico = dico
+        self.bc = Boundary(self.domain, dico)
+        for meth in self.bc.methods:
+            meth.set_iload()
+        self.t = 0.0
+        self.nt = 0
+        self.dt = self.domain.dx / sc.la_float
+        self._ready = False
+
+    def extra_parameters_str(self):
+        return {str(k): v for k, v in self.extra_parameters.items()}
+
+    def _tables(self):
+        sc = self.scheme
+        s = sc.rates_numpy(self.extra_parameters_str())
+        rows, coefs, expos = equilibrium_table(sc, self.extra_parameters_str())
+        return np.ascontiguousarray(s), rows, coefs, expos
+
+    def initialize(self):
+        sc = self.scheme
+        coords = np.meshgrid(*self.domain.coords_halo, sparse=True, indexing="ij")
+        m = np.zeros_like(self.f)
+        init_type = self.dico.get("inittype", "moments")
+        for key, val in (self.dico.get("init") or {}).items():
+            idx = sc.consm[key] if init_type == "moments" and isinstance(key, sp.Basic) else int(key)
+            if isinstance(val, tuple):
+                m[idx] = val[0](*(tuple(coords) + (tuple(val[1]) if len(val) == 2 else ())))
+            elif callable(val):
+                m[idx] = val(*coords)
+            else:
+                m[idx] = val
+        s, rows, coefs, expos = self._tables()
+        if init_type == "moments":
+            lib().oracle_equilibrium(_p(m), self.dim, sc.nv, sc.nconsm, _p(self.n), _p(self.h), len(rows), _p(rows),
+                                     _p(coefs), _p(expos))
+            lib().oracle_m2f(_p(m), _p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h), _p(self.invM))
+        else:
+            self.f[...] = m
+        self.fnew[...] = self.f
+        for meth in self.bc.methods:
+            meth.prepare_rhs(self)
+            meth.fix_iload()
+            meth.set_rhs()
+        self._ready = True
+
+    def one_time_step(self):
+        if not self._ready:
+            self.initialize()
+        sc = self.scheme
+        L = lib()
+        L.oracle_update_halo(_p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h))
+        for meth in self.bc.methods:
+            if meth.update_feq(self):
+                meth.set_rhs()
+            sign = -1.0 if meth.kind == "anti_bounce_back" else 1.0
+            rhs = meth.rhs if meth.kind != "neumann" else None
+            L.oracle_boundary(_p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h), _p(meth.iload[0]),
+                              _p(meth.istore), meth.ncond, _p(rhs) if rhs is not None else None, sign)
+        s, rows, coefs, expos = self._tables()
+        L.oracle_one_time_step(_p(self.f), _p(self.fnew), self.dim, sc.nv, sc.nconsm, _p(self.n), _p(self.h),
+                               _p(self.vel), _p(self.M), _p(self.invM), _p(s), len(rows), _p(rows), _p(coefs),
+                               _p(expos), self.nthreads)
+        self.f, self.fnew = self.fnew, self.f
+        self.t += self.dt
+        self.nt += 1
+
+    def run(self, nsteps):
+        for _ in range(int(nsteps)):
+            self.one_time_step()
+
+    def moments_halo(self):
+        sc = self.scheme
+        m = np.zeros_like(self.f)
+        lib().oracle_f2m(_p(self.f), _p(m), self.dim, sc.nv, _p(self.n), _p(self.h), _p(self.M))
+        return m
+
+    def moments(self):
+        inner = (slice(None),) + tuple(slice(int(h), -int(h)) for h in self.h)
+        return self.moments_halo()[inner]
+
+    # boundary methods call back into these (prepare_rhs / update_feq)
+    @property
+    def _mlist(self):
+        return None

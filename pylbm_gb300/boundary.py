@@ -1,0 +1,260 @@
+"""Boundary link lists and boundary methods (pylbm/boundary.py).
+
+Link lists are built on the host once, exactly as the reference builds them:
+for every label and every velocity k of a scheme, the fluid nodes x whose link
+x -> x - v_k crosses a wall with that label give a store slot (k, x - v_k) in a
+ghost or solid node (pylbm/boundary.py:23-47 ``BoundaryVelocity``); slots are
+grouped per method class in the order labels, schemes, velocities are met
+(:78-160).  Each method derives its load slots (``set_iload``) and its
+right-hand side from the equilibrium at the wall points (``prepare_rhs``,
+:238-305).  The lists are uploaded once; every step the device kernels of the
+C ABI apply ``f[istore] = +/- f[iload0] + rhs``.
+"""
+from collections import OrderedDict
+
+import numpy as np
+import sympy as sp
+
+
+class _BoundaryVelocity:
+    """Store slots of one label for one incoming velocity (pylbm/boundary.py:23-47)."""
+
+    def __init__(self, domain, label, kunique):
+        st = domain.stencil
+        v = st.unique_v[kunique]
+        vsym = -v
+        from .stencil import velocity_number
+        num = velocity_number(tuple(int(c) for c in vsym))
+        ksym_u = int(st.unum2index[num])
+        ind = np.where(domain.flag[ksym_u] == label)
+        self.indices = np.array(ind, dtype=np.int64)
+        if self.indices.size:
+            self.indices = self.indices + vsym[:, np.newaxis]
+        self.distance = np.array(domain.distance[(ksym_u,) + ind])
+
+
+class _Moments:
+    """Moment container handed to user boundary functions (``m[RHO] = ...``)."""
+
+    def __init__(self, array, consm):
+        self.array = array
+        self.consm = consm
+
+    def _key(self, key):
+        if isinstance(key, (sp.Symbol, sp.IndexedBase)):
+            return self.consm[key]
+        if isinstance(key, str) and sp.Symbol(key) in self.consm:
+            return self.consm[sp.Symbol(key)]
+        return key
+
+    def __getitem__(self, key):
+        return self.array[self._key(key)]
+
+    def __setitem__(self, key, value):
+        self.array[self._key(key)] = value
+
+
+class BoundaryMethod:
+    """Common part of the boundary methods (pylbm/boundary.py:164-397).
+
+    ``kind`` selects the device kernel: 'bounce_back', 'anti_bounce_back' or
+    'neumann'.
+    """
+
+    kind = None
+    name = None
+
+    def __init__(self, istore, ilabel, distance, stencil, value_bc, time_bc):
+        self.istore = istore            # (dim+1, ncond) until fix_iload
+        self.ilabel = ilabel
+        self.distance = distance
+        self.stencil = stencil
+        self.feq = np.zeros((stencil.nvtot, istore.shape[1]))
+        self.rhs = np.zeros(istore.shape[1])
+        self.value_bc = {k: value_bc[k] for k in np.unique(ilabel)}
+        self.time_bc = {k: time_bc[k] for k in np.unique(ilabel)}
+        self.iload = []
+        self._timed = []
+        self.ncond = int(istore.shape[1])
+
+    def set_iload(self):
+        raise NotImplementedError
+
+    def set_rhs(self):
+        pass
+
+    def fix_iload(self):
+        """(dim+1, ncond) -> contiguous (ncond, dim+1) int32 (pylbm/boundary.py:226-235)."""
+        self.iload = [np.ascontiguousarray(il.T, dtype=np.int32) for il in self.iload]
+        self.istore = np.ascontiguousarray(self.istore.T, dtype=np.int32)
+
+    def _wall_points(self, sim, sel):
+        """Wall point of every selected link: x_g + (1 - distance) v_k dx."""
+        dim = sim.domain.dim
+        k = self.istore[0, sel]
+        s = 1.0 - self.distance[sel]
+        v = self.stencil.get_all_velocities()
+        coords = []
+        for d in range(dim):
+            x = sim.domain.coords_halo[d][self.istore[d + 1, sel]] + s * v[k, d] * sim.domain.dx
+            x = x.ravel()
+            for _ in range(1, dim):
+                x = x[:, np.newaxis]
+            coords.append(x)
+        return coords
+
+    def _eval_value(self, sim, func, args, sel, t=None):
+        n = sel.size
+        shape = [sim.scheme.nv, n] + [1] * (sim.domain.dim - 1)
+        m = _Moments(np.zeros(shape), sim.scheme.consm)
+        f = _Moments(np.zeros(shape), sim.scheme.consm)
+        if t is None:
+            func(f, m, *args)
+        else:
+            func(f, m, t, *args)
+        cons = m.array.reshape(sim.scheme.nv, n)[:sim.scheme.nconsm]
+        return sim.scheme.feq_numpy(cons, sim.extra_parameters_str())
+
+    def prepare_rhs(self, sim):
+        """Equilibrium populations at the wall points of labels with a value."""
+        self._timed = []
+        for label, value in self.value_bc.items():
+            if value is None:
+                continue
+            sel = np.where(self.ilabel == label)[0]
+            coords = self._wall_points(sim, sel)
+            func, extra = (value[0], tuple(value[1]) if len(value) > 1 else ()) if isinstance(value, tuple) else (value, ())
+            args = tuple(coords) + extra
+            t = 0.0 if self.time_bc[label] else None
+            self.feq[:, sel] = self._eval_value(sim, func, args, sel, t)
+            if self.time_bc[label]:
+                self._timed.append((func, args, sel))
+
+    def update_feq(self, sim):
+        """Re-evaluate time-dependent boundary values (pylbm/boundary.py:307-321)."""
+        for func, args, sel in self._timed:
+            self.feq[:, sel] = self._eval_value(sim, func, args, sel, sim.t)
+        return bool(self._timed)
+
+
+class BounceBack(BoundaryMethod):
+    """f_k(x_g) = f_k'(x_g + v_k) + feq_k - feq_k'  (pylbm/boundary.py:400-469)."""
+
+    kind = "bounce_back"
+    name = "bounce_back"
+
+    def set_iload(self):
+        k = self.istore[0]
+        ksym = self.stencil.get_symmetric()[k][np.newaxis, :]
+        v = self.stencil.get_all_velocities()
+        self.iload.append(np.concatenate([ksym, self.istore[1:] + v[k].T]))
+
+    def set_rhs(self):
+        k = self.istore[:, 0]
+        ksym = self.stencil.get_symmetric()[k]
+        i = np.arange(k.size)
+        self.rhs[:] = self.feq[k, i] - self.feq[ksym, i]
+
+
+class AntiBounceBack(BounceBack):
+    """f_k(x_g) = -f_k'(x_g + v_k) + feq_k + feq_k'  (pylbm/boundary.py:626-684)."""
+
+    kind = "anti_bounce_back"
+    name = "anti_bounce_back"
+
+    def set_rhs(self):
+        k = self.istore[:, 0]
+        ksym = self.stencil.get_symmetric()[k]
+        i = np.arange(k.size)
+        self.rhs[:] = self.feq[k, i] + self.feq[ksym, i]
+
+
+class Neumann(BoundaryMethod):
+    """f_k(x_g) = f_k(x_g + v_k)  (pylbm/boundary.py:763-823)."""
+
+    kind = "neumann"
+    name = "neumann"
+
+    def set_iload(self):
+        k = self.istore[0]
+        v = self.stencil.get_all_velocities()
+        self.iload.append(np.concatenate([k[np.newaxis, :], self.istore[1:] + v[k].T]))
+
+
+class _NeumannAxis(Neumann):
+    axis = 0
+
+    def set_iload(self):
+        k = self.istore[0]
+        v = self.stencil.get_all_velocities()
+        ind = self.istore[1:].copy()
+        ind[self.axis] += v[k].T[self.axis]
+        self.iload.append(np.concatenate([k[np.newaxis, :], ind]))
+
+
+class NeumannX(_NeumannAxis):
+    """Neumann along x only (pylbm/boundary.py:826-847)."""
+    name = "neumannx"
+    axis = 0
+
+
+class NeumannY(_NeumannAxis):
+    """Neumann along y only (pylbm/boundary.py:850-871)."""
+    name = "neumanny"
+    axis = 1
+
+
+class NeumannZ(_NeumannAxis):
+    """Neumann along z only (pylbm/boundary.py:874-895)."""
+    name = "neumannz"
+    axis = 2
+
+
+_BY_NAME = {c.__name__: c for c in (BounceBack, AntiBounceBack, Neumann, NeumannX, NeumannY, NeumannZ)}
+
+
+def resolve_method(cls):
+    """Map a pylbm boundary class (or one of ours) to this module's class by name."""
+    if isinstance(cls, type) and issubclass(cls, BoundaryMethod):
+        return cls
+    name = getattr(cls, "__name__", str(cls))
+    if name in _BY_NAME:
+        return _BY_NAME[name]
+    raise NotImplementedError(f"boundary method {name} is not supported by the CUDA backend")
+
+
+class Boundary:
+    """Boundary link lists per method (pylbm/boundary.py:50-160)."""
+
+    def __init__(self, domain, dico):
+        self.domain = domain
+        st = domain.stencil
+        labels = [int(l) for l in domain.list_of_labels() if int(l) not in (-1, -2)]
+        bv = {lab: [_BoundaryVelocity(domain, lab, k) for k in range(st.unvtot)] for lab in labels}
+        dico_bound = dico.get("boundary_conditions", {}) or {}
+        istore = OrderedDict()
+        ilabel, distance = {}, {}
+        value_bc, time_bc = {}, {}
+        for lab in labels:
+            if lab not in dico_bound:
+                raise ValueError(f"no boundary condition given for label {lab}")
+            value_bc[lab] = dico_bound[lab].get("value", None)
+            time_bc[lab] = dico_bound[lab].get("time_bc", False)
+            for ksch, cls in dico_bound[lab]["method"].items():
+                meth = resolve_method(cls)
+                for inum, num in enumerate(st.num(ksch)):
+                    b = bv[lab][int(st.unum2index[num])]
+                    if b.indices.size == 0:
+                        continue
+                    n = b.indices.shape[1]
+                    vel = (inum + int(st.nv_ptr[ksch])) * np.ones((1, n), dtype=np.int64)
+                    block = np.concatenate([vel, b.indices])
+                    if meth not in istore:
+                        istore[meth] = block.copy()
+                        ilabel[meth] = lab * np.ones(n, dtype=np.int64)
+                        distance[meth] = b.distance.copy()
+                    else:
+                        istore[meth] = np.concatenate([istore[meth], block], axis=1)
+                        ilabel[meth] = np.concatenate([ilabel[meth], lab * np.ones(n, dtype=np.int64)])
+                        distance[meth] = np.concatenate([distance[meth], b.distance])
+        self.methods = [cls(istore[cls], ilabel[cls], distance[cls], st, value_bc, time_bc) for cls in istore]

@@ -1,0 +1,149 @@
+// Shared device helpers: storage conversions, the lattice geometry passed by
+// value to kernels, and the per-thread error message used by both libraries.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+
+#include "lbm_gb300.h"
+
+namespace lbm {
+
+// ---------------------------------------------------------------- errors
+struct ErrorSlot {
+  char msg[512];
+};
+
+inline ErrorSlot& error_slot() {
+  static thread_local ErrorSlot slot = {{0}};
+  return slot;
+}
+
+inline int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(error_slot().msg, sizeof(error_slot().msg), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+inline int cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    return fail(LBM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+  return LBM_OK;
+}
+
+inline int launch_check(const char* what) {
+  return cuda_check(cudaGetLastError(), what);
+}
+
+inline size_t dtype_size(int dt) {
+  switch (dt) {
+    case LBM_F64: return 8;
+    case LBM_F32: return 4;
+    case LBM_F16: return 2;
+    case LBM_BF16: return 2;
+    default: return 0;
+  }
+}
+
+// ---------------------------------------------------------------- storage
+template <typename S> struct Store;
+
+template <> struct Store<double> {
+  static constexpr int code = LBM_F64;
+  __device__ __forceinline__ static double load(const double* p) { return __ldg(p); }
+  __device__ __forceinline__ static double load_plain(const double* p) { return *p; }
+  __device__ __forceinline__ static void store(double* p, double v) { *p = v; }
+};
+
+template <> struct Store<float> {
+  static constexpr int code = LBM_F32;
+  __device__ __forceinline__ static float load(const float* p) { return __ldg(p); }
+  __device__ __forceinline__ static float load_plain(const float* p) { return *p; }
+  __device__ __forceinline__ static void store(float* p, float v) { *p = v; }
+};
+
+template <> struct Store<__half> {
+  static constexpr int code = LBM_F16;
+  __device__ __forceinline__ static float load(const __half* p) { return __half2float(__ldg(p)); }
+  __device__ __forceinline__ static float load_plain(const __half* p) { return __half2float(*p); }
+  __device__ __forceinline__ static void store(__half* p, float v) { *p = __float2half_rn(v); }
+};
+
+template <> struct Store<__nv_bfloat16> {
+  static constexpr int code = LBM_BF16;
+  __device__ __forceinline__ static float load(const __nv_bfloat16* p) {
+    return __bfloat162float(__ldg(p));
+  }
+  __device__ __forceinline__ static float load_plain(const __nv_bfloat16* p) {
+    return __bfloat162float(*p);
+  }
+  __device__ __forceinline__ static void store(__nv_bfloat16* p, float v) {
+    *p = __float2bfloat16_rn(v);
+  }
+};
+
+// ---------------------------------------------------------------- geometry
+// Kernel-side copy of lbm_lattice (without the shift table).
+struct Geo {
+  int dim;
+  int nv;
+  int n[3];
+  int h[3];
+  long long stride[3];
+  long long vstride;
+  long long origin;
+};
+
+inline Geo make_geo(const lbm_lattice& l) {
+  Geo g;
+  g.dim = l.dim;
+  g.nv = l.nv;
+  for (int d = 0; d < 3; ++d) {
+    g.n[d] = l.n[d];
+    g.h[d] = l.halo[d];
+    g.stride[d] = l.stride[d];
+  }
+  g.vstride = l.vstride;
+  g.origin = l.origin;
+  return g;
+}
+
+// Validate a lattice descriptor against its own invariants.
+inline int check_lattice(const lbm_lattice* l, const char* who) {
+  if (!l) return fail(LBM_ERR_ARG, "%s: lattice is NULL", who);
+  if (l->dim < 1 || l->dim > 3) return fail(LBM_ERR_ARG, "%s: dim=%d", who, l->dim);
+  if (l->nv < 1 || l->nv > LBM_MAX_Q) return fail(LBM_ERR_ARG, "%s: nv=%d", who, l->nv);
+  if (dtype_size(l->dtype) == 0) return fail(LBM_ERR_ARG, "%s: dtype=%d", who, l->dtype);
+  for (int d = 0; d < 3; ++d) {
+    if (l->n[d] < 1) return fail(LBM_ERR_ARG, "%s: n[%d]=%d", who, d, l->n[d]);
+    if (l->halo[d] < 0) return fail(LBM_ERR_ARG, "%s: halo[%d]=%d", who, d, l->halo[d]);
+    if (d < l->dim && l->halo[d] > l->n[d])
+      return fail(LBM_ERR_ARG, "%s: halo[%d]=%d exceeds n=%d", who, d, l->halo[d], l->n[d]);
+    if (d >= l->dim && (l->n[d] != 1 || l->halo[d] != 0))
+      return fail(LBM_ERR_ARG, "%s: unused axis %d must have n=1, halo=0", who, d);
+  }
+  if (l->stride[l->dim - 1] != 1) return fail(LBM_ERR_ARG, "%s: last axis must be contiguous", who);
+  // the last element of the last population must lie inside the allocation
+  long long last = (long long)(l->nv - 1) * l->vstride + l->origin;
+  for (int d = 0; d < l->dim; ++d) last += (long long)(l->n[d] + 2 * l->halo[d] - 1) * l->stride[d];
+  if (l->origin < 0 || last >= l->elements)
+    return fail(LBM_ERR_ARG, "%s: strides exceed the allocation (%lld >= %lld)", who, last,
+                (long long)l->elements);
+  return LBM_OK;
+}
+
+// Element offset of halo coordinates (i0, i1, i2) of population 0.
+__host__ __device__ __forceinline__ long long node_offset(const Geo& g, int i0, int i1, int i2) {
+  return g.origin + (long long)i0 * g.stride[0] + (long long)i1 * g.stride[1] +
+         (long long)i2 * g.stride[2];
+}
+
+}  // namespace lbm

@@ -1,0 +1,465 @@
+// liblbm_gb300.so: scheme-independent runtime of the GB300 pylbm backend.
+//
+// Device memory, streams, the periodic ghost refresh, the boundary-node
+// kernels and FP64 conservation sums.  Everything is reached through the C
+// ABI declared in include/lbm_gb300.h.
+#include "lbm_common.cuh"
+
+#include <cstring>
+#include <type_traits>
+
+using namespace lbm;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------- halo
+// Slab decomposition of the ghost shell: slab (axis a, side s) holds the
+// h[a] ghost layers of that side with every other axis at full halo extent.
+// Cells at edges and corners belong to several slabs; each slab writes the
+// same value there (the fully wrapped interior node), so the overlap is benign
+// and the result equals pylbm's sequential x-then-y-then-z exchange.
+struct HaloPlan {
+  long long slab_cells[6];
+  long long slab_begin[7];
+  int nslab;
+};
+
+__device__ __forceinline__ int wrap_index(int i, int n, int h) {
+  if (i < h) return i + n;
+  if (i >= n + h) return i - n;
+  return i;
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_update_halo(S* __restrict__ f, Geo g, HaloPlan p) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.slab_begin[p.nslab]) return;
+  int k = blockIdx.y;
+  int slab = 0;
+  while (slab + 1 < p.nslab && t >= p.slab_begin[slab + 1]) ++slab;
+  long long r = t - p.slab_begin[slab];
+  int axis = slab >> 1, side = slab & 1;
+  int ext[3], idx[3];
+  for (int d = 0; d < 3; ++d) ext[d] = g.n[d] + 2 * g.h[d];
+  ext[axis] = g.h[axis];
+  // decompose r with the last axis fastest
+  for (int d = 2; d >= 0; --d) {
+    idx[d] = (int)(r % ext[d]);
+    r /= ext[d];
+  }
+  if (side) idx[axis] += g.n[axis] + g.h[axis];
+  int src[3];
+  for (int d = 0; d < 3; ++d) src[d] = (d < g.dim) ? wrap_index(idx[d], g.n[d], g.h[d]) : idx[d];
+  long long o_dst = (long long)k * g.vstride + node_offset(g, idx[0], idx[1], idx[2]);
+  long long o_src = (long long)k * g.vstride + node_offset(g, src[0], src[1], src[2]);
+  f[o_dst] = f[o_src];
+}
+
+// ---------------------------------------------------------------- boundary
+struct BcArgs {
+  const int* iload;
+  const int* istore;
+  const double* rhs;
+  int ncond;
+  double sign;  // +1 bounce-back / Neumann, -1 anti-bounce-back
+  double shift[LBM_MAX_Q];
+};
+
+template <typename S>
+__device__ __forceinline__ void bc_link(S* f, const Geo& g, const BcArgs& a, int c) {
+  const int w = g.dim + 1;
+  const int* st = a.istore + (long long)c * w;
+  const int* ld = a.iload + (long long)c * w;
+  int is[3] = {0, 0, 0}, il[3] = {0, 0, 0};
+  for (int d = 0; d < g.dim; ++d) {
+    is[d] = st[1 + d];
+    il[d] = ld[1 + d];
+  }
+  const int ks = st[0], kl = ld[0];
+  long long os = (long long)ks * g.vstride + node_offset(g, is[0], is[1], is[2]);
+  long long ol = (long long)kl * g.vstride + node_offset(g, il[0], il[1], il[2]);
+  double fl = (double)Store<S>::load_plain(f + ol) + a.shift[kl];
+  double v = a.sign * fl + (a.rhs ? a.rhs[c] : 0.0);
+  Store<S>::store(f + os, (decltype(Store<S>::load_plain(f)))(v - a.shift[ks]));
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_boundary(S* __restrict__ f, Geo g, BcArgs a) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < a.ncond) bc_link(f, g, a, c);
+}
+
+// one thread, links in list order: the reference's sequential semantics
+template <typename S>
+__global__ void k_boundary_ordered(S* __restrict__ f, Geo g, BcArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    for (int c = 0; c < a.ncond; ++c) bc_link(f, g, a, c);
+}
+
+// ---------------------------------------------------------------- sums
+// Stage 1: block b of population k sums rows [b*rows_per_block, ...) of the
+// interior with FP64 warp shuffles; stage 2 adds the per-block partials.
+struct SumPlan {
+  long long rows;           // interior rows (all axes but the last)
+  long long rows_per_block;
+  int blocks;               // per population
+  int row_len;              // interior length of the last axis
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_sums_stage1(const S* __restrict__ f, Geo g, SumPlan p,
+                                                          double* __restrict__ partials,
+                                                          int* __restrict__ nonfinite) {
+  const int k = blockIdx.y;
+  const int L = g.dim - 1;
+  double acc = 0.0;
+  bool bad = false;
+  long long r0 = (long long)blockIdx.x * p.rows_per_block;
+  long long r1 = r0 + p.rows_per_block;
+  if (r1 > p.rows) r1 = p.rows;
+  for (long long r = r0; r < r1; ++r) {
+    // row r -> interior coordinates of the axes before the last
+    int idx[3] = {0, 0, 0};
+    long long q = r;
+    for (int d = L - 1; d >= 0; --d) {
+      idx[d] = (int)(q % g.n[d]) + g.h[d];
+      q /= g.n[d];
+    }
+    idx[L] = g.h[L];
+    const S* row = f + (long long)k * g.vstride + node_offset(g, idx[0], idx[1], idx[2]);
+    for (int i = threadIdx.x; i < p.row_len; i += blockDim.x) {
+      double v = (double)Store<S>::load(row + i);
+      bad |= !isfinite(v);
+      acc += v;
+    }
+  }
+  __shared__ double red[kThreads / 32];
+  __shared__ int badflag;
+  if (threadIdx.x == 0) badflag = 0;
+  __syncthreads();
+  if (bad) atomicOr(&badflag, 1);
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (kThreads / 32) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) {
+      partials[(long long)k * p.blocks + blockIdx.x] = v;
+      if (badflag) atomicAdd(nonfinite, 1);
+    }
+  }
+}
+
+struct ShiftTable {
+  double v[LBM_MAX_Q];
+};
+
+__global__ void __launch_bounds__(kThreads) k_sums_stage2(const double* __restrict__ partials, int blocks,
+                                                          long long count, ShiftTable shift,
+                                                          double* __restrict__ sums) {
+  const int k = blockIdx.x;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < blocks; i += blockDim.x) acc += partials[(long long)k * blocks + i];
+  __shared__ double red[kThreads / 32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (kThreads / 32) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) sums[k] = v + (double)count * shift.v[k];
+  }
+}
+
+SumPlan make_sum_plan(const lbm_lattice& l) {
+  SumPlan p;
+  const int L = l.dim - 1;
+  p.row_len = l.n[L];
+  p.rows = 1;
+  for (int d = 0; d < L; ++d) p.rows *= l.n[d];
+  // about 8 rows of work per block, at most 4096 blocks per population
+  long long target = (p.rows + 4095) / 4096;
+  long long per = target > 8 ? target : 8;
+  if (per > p.rows) per = p.rows;
+  p.rows_per_block = per;
+  p.blocks = (int)((p.rows + per - 1) / per);
+  return p;
+}
+
+template <typename F>
+int dispatch_dtype(int dt, F&& fn) {
+  switch (dt) {
+    case LBM_F64: return fn((double*)nullptr);
+    case LBM_F32: return fn((float*)nullptr);
+    case LBM_F16: return fn((__half*)nullptr);
+    case LBM_BF16: return fn((__nv_bfloat16*)nullptr);
+    default: return fail(LBM_ERR_ARG, "unknown dtype %d", dt);
+  }
+}
+
+int boundary_common(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
+                    const double* rhs, const lbm_lattice* lat, int32_t ordered, double sign,
+                    const char* who, void* stream) {
+  int rc = check_lattice(lat, who);
+  if (rc) return rc;
+  if (ncond < 0) return fail(LBM_ERR_ARG, "%s: ncond=%d", who, ncond);
+  if (ncond == 0) return LBM_OK;
+  if (!f || !iload0 || !istore) return fail(LBM_ERR_ARG, "%s: NULL array", who);
+  BcArgs a;
+  a.iload = iload0;
+  a.istore = istore;
+  a.rhs = rhs;
+  a.ncond = ncond;
+  a.sign = sign;
+  for (int k = 0; k < LBM_MAX_Q; ++k) a.shift[k] = k < lat->nv ? lat->shift[k] : 0.0;
+  Geo g = make_geo(*lat);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    if (ordered) {
+      k_boundary_ordered<S><<<1, 1, 0, s>>>((S*)f, g, a);
+    } else {
+      int blocks = (ncond + kThreads - 1) / kThreads;
+      k_boundary<S><<<blocks, kThreads, 0, s>>>((S*)f, g, a);
+    }
+    return launch_check(who);
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm_version(void) { return "pylbm_gb300 0.1.0 (sm_103a)"; }
+
+const char* lbm_last_error(void) { return error_slot().msg; }
+
+int lbm_lattice_init(lbm_lattice* lat, int32_t dim, int32_t nv, int32_t dtype, const int32_t* n,
+                     const int32_t* halo) {
+  if (!lat || !n || !halo) return fail(LBM_ERR_ARG, "lbm_lattice_init: NULL argument");
+  if (dim < 1 || dim > 3) return fail(LBM_ERR_ARG, "lbm_lattice_init: dim=%d", dim);
+  if (nv < 1 || nv > LBM_MAX_Q) return fail(LBM_ERR_ARG, "lbm_lattice_init: nv=%d", nv);
+  size_t es = dtype_size(dtype);
+  if (!es) return fail(LBM_ERR_ARG, "lbm_lattice_init: dtype=%d", dtype);
+  std::memset(lat, 0, sizeof(*lat));
+  lat->dim = dim;
+  lat->nv = nv;
+  lat->dtype = dtype;
+  for (int d = 0; d < 3; ++d) {
+    lat->n[d] = d < dim ? n[d] : 1;
+    lat->halo[d] = d < dim ? halo[d] : 0;
+    if (lat->n[d] < 1 || lat->halo[d] < 0)
+      return fail(LBM_ERR_ARG, "lbm_lattice_init: n[%d]=%d halo[%d]=%d", d, lat->n[d], d, lat->halo[d]);
+  }
+  const long long align = (long long)(32 / es);  // 32-byte rows
+  const int L = dim - 1;
+  const long long h = lat->halo[L];
+  const long long lead = ((h + align - 1) / align) * align;
+  const long long pitch = ((lead + lat->n[L] + h + align - 1) / align) * align;
+  long long s = pitch;
+  for (int d = 2; d >= 0; --d) {
+    if (d > L) {
+      lat->stride[d] = 0;
+    } else if (d == L) {
+      lat->stride[d] = 1;
+    } else {
+      lat->stride[d] = s;
+      s *= (long long)(lat->n[d] + 2 * lat->halo[d]);
+    }
+  }
+  long long box = (L == 0) ? pitch : s;
+  const long long valign = 128 / (long long)es;  // populations start on 128-byte boundaries
+  lat->vstride = ((box + valign - 1) / valign) * valign;
+  lat->origin = lead - h;
+  lat->elements = (long long)nv * lat->vstride;
+  return LBM_OK;
+}
+
+int lbm_device_count(int32_t* count) {
+  int c = 0;
+  int rc = cuda_check(cudaGetDeviceCount(&c), "cudaGetDeviceCount");
+  if (count) *count = rc ? 0 : c;
+  return rc;
+}
+
+int lbm_set_device(int32_t device) { return cuda_check(cudaSetDevice(device), "cudaSetDevice"); }
+
+int lbm_device_synchronize(void) { return cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize"); }
+
+int lbm_alloc(void** ptr, size_t bytes) {
+  if (!ptr) return fail(LBM_ERR_ARG, "lbm_alloc: NULL ptr");
+  *ptr = nullptr;
+  if (bytes == 0) bytes = 256;
+  return cuda_check(cudaMalloc(ptr, bytes), "cudaMalloc");
+}
+
+int lbm_free(void* ptr) {
+  if (!ptr) return LBM_OK;
+  return cuda_check(cudaFree(ptr), "cudaFree");
+}
+
+int lbm_memcpy(void* dst, const void* src, size_t bytes, int32_t kind, void* stream) {
+  if (bytes == 0) return LBM_OK;
+  if (!dst || !src) return fail(LBM_ERR_ARG, "lbm_memcpy: NULL pointer");
+  cudaMemcpyKind k;
+  switch (kind) {
+    case LBM_H2D: k = cudaMemcpyHostToDevice; break;
+    case LBM_D2H: k = cudaMemcpyDeviceToHost; break;
+    case LBM_D2D: k = cudaMemcpyDeviceToDevice; break;
+    default: return fail(LBM_ERR_ARG, "lbm_memcpy: kind=%d", kind);
+  }
+  return cuda_check(cudaMemcpyAsync(dst, src, bytes, k, (cudaStream_t)stream), "cudaMemcpyAsync");
+}
+
+int lbm_memset(void* ptr, int32_t value, size_t bytes, void* stream) {
+  if (bytes == 0) return LBM_OK;
+  if (!ptr) return fail(LBM_ERR_ARG, "lbm_memset: NULL pointer");
+  return cuda_check(cudaMemsetAsync(ptr, value, bytes, (cudaStream_t)stream), "cudaMemsetAsync");
+}
+
+int lbm_stream_create(void** stream) {
+  if (!stream) return fail(LBM_ERR_ARG, "lbm_stream_create: NULL");
+  cudaStream_t s;
+  int rc = cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+  *stream = rc ? nullptr : (void*)s;
+  return rc;
+}
+
+int lbm_stream_destroy(void* stream) {
+  if (!stream) return LBM_OK;
+  return cuda_check(cudaStreamDestroy((cudaStream_t)stream), "cudaStreamDestroy");
+}
+
+int lbm_stream_synchronize(void* stream) {
+  return cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+}
+
+int lbm_host_alloc(void** ptr, size_t bytes) {
+  if (!ptr) return fail(LBM_ERR_ARG, "lbm_host_alloc: NULL ptr");
+  *ptr = nullptr;
+  return cuda_check(cudaMallocHost(ptr, bytes ? bytes : 256), "cudaMallocHost");
+}
+
+int lbm_host_free(void* ptr) {
+  if (!ptr) return LBM_OK;
+  return cuda_check(cudaFreeHost(ptr), "cudaFreeHost");
+}
+
+int lbm_event_create(void** event) {
+  if (!event) return fail(LBM_ERR_ARG, "lbm_event_create: NULL");
+  cudaEvent_t e;
+  int rc = cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+  *event = rc ? nullptr : (void*)e;
+  return rc;
+}
+
+int lbm_event_destroy(void* event) {
+  if (!event) return LBM_OK;
+  return cuda_check(cudaEventDestroy((cudaEvent_t)event), "cudaEventDestroy");
+}
+
+int lbm_event_record(void* event, void* stream) {
+  if (!event) return fail(LBM_ERR_ARG, "lbm_event_record: NULL event");
+  return cuda_check(cudaEventRecord((cudaEvent_t)event, (cudaStream_t)stream), "cudaEventRecord");
+}
+
+int lbm_event_elapsed_ms(void* start, void* end, float* ms) {
+  if (!start || !end || !ms) return fail(LBM_ERR_ARG, "lbm_event_elapsed_ms: NULL");
+  int rc = cuda_check(cudaEventSynchronize((cudaEvent_t)end), "cudaEventSynchronize");
+  if (rc) return rc;
+  return cuda_check(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)end), "cudaEventElapsedTime");
+}
+
+int lbm_update_halo(void* f, const lbm_lattice* lat, void* stream) {
+  int rc = check_lattice(lat, "lbm_update_halo");
+  if (rc) return rc;
+  if (!f) return fail(LBM_ERR_ARG, "lbm_update_halo: f is NULL");
+  HaloPlan p;
+  p.nslab = 0;
+  p.slab_begin[0] = 0;
+  for (int a = 0; a < lat->dim; ++a) {
+    long long cells = lat->halo[a];
+    for (int d = 0; d < 3; ++d)
+      if (d != a) cells *= (long long)(lat->n[d] + 2 * lat->halo[d]);
+    for (int side = 0; side < 2; ++side) {
+      p.slab_cells[p.nslab] = cells;
+      p.slab_begin[p.nslab + 1] = p.slab_begin[p.nslab] + cells;
+      ++p.nslab;
+    }
+  }
+  long long total = p.slab_begin[p.nslab];
+  if (total == 0) return LBM_OK;
+  Geo g = make_geo(*lat);
+  dim3 grid((unsigned)((total + kThreads - 1) / kThreads), (unsigned)lat->nv);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    k_update_halo<S><<<grid, kThreads, 0, s>>>((S*)f, g, p);
+    return launch_check("lbm_update_halo");
+  });
+}
+
+int lbm_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
+                    const double* rhs, const lbm_lattice* lat, int32_t ordered, void* stream) {
+  return boundary_common(f, iload0, istore, ncond, rhs, lat, ordered, 1.0, "lbm_bounce_back", stream);
+}
+
+int lbm_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
+                         const double* rhs, const lbm_lattice* lat, int32_t ordered, void* stream) {
+  return boundary_common(f, iload0, istore, ncond, rhs, lat, ordered, -1.0, "lbm_anti_bounce_back",
+                         stream);
+}
+
+int lbm_neumann(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
+                const lbm_lattice* lat, int32_t ordered, void* stream) {
+  return boundary_common(f, iload0, istore, ncond, nullptr, lat, ordered, 1.0, "lbm_neumann", stream);
+}
+
+int lbm_population_sums_scratch_bytes(const lbm_lattice* lat, size_t* bytes) {
+  int rc = check_lattice(lat, "lbm_population_sums_scratch_bytes");
+  if (rc) return rc;
+  if (!bytes) return fail(LBM_ERR_ARG, "lbm_population_sums_scratch_bytes: NULL");
+  SumPlan p = make_sum_plan(*lat);
+  // one FP64 partial sum per block and population
+  *bytes = (size_t)lat->nv * (size_t)p.blocks * sizeof(double);
+  return LBM_OK;
+}
+
+int lbm_population_sums(const void* f, const lbm_lattice* lat, double* sums, int32_t* nonfinite,
+                        void* partials, size_t partials_bytes, void* stream) {
+  int rc = check_lattice(lat, "lbm_population_sums");
+  if (rc) return rc;
+  if (!f || !sums || !nonfinite || !partials) return fail(LBM_ERR_ARG, "lbm_population_sums: NULL");
+  size_t need = 0;
+  lbm_population_sums_scratch_bytes(lat, &need);
+  if (partials_bytes < need)
+    return fail(LBM_ERR_ARG, "lbm_population_sums: scratch has %zu bytes, needs %zu", partials_bytes, need);
+  SumPlan p = make_sum_plan(*lat);
+  cudaStream_t s = (cudaStream_t)stream;
+  double* part = (double*)partials;
+  ShiftTable shift;
+  for (int k = 0; k < LBM_MAX_Q; ++k) shift.v[k] = k < lat->nv ? lat->shift[k] : 0.0;
+  rc = cuda_check(cudaMemsetAsync(nonfinite, 0, sizeof(int32_t), s), "lbm_population_sums: clear flag");
+  if (rc) return rc;
+  long long count = p.rows * (long long)p.row_len;
+  Geo g = make_geo(*lat);
+  rc = dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    dim3 grid((unsigned)p.blocks, (unsigned)lat->nv);
+    k_sums_stage1<S><<<grid, kThreads, 0, s>>>((const S*)f, g, p, part, (int*)nonfinite);
+    return launch_check("lbm_population_sums stage 1");
+  });
+  if (rc) return rc;
+  k_sums_stage2<<<lat->nv, kThreads, 0, s>>>(part, p.blocks, count, shift, sums);
+  return launch_check("lbm_population_sums stage 2");
+}
+
+}  // extern "C"

@@ -1,0 +1,360 @@
+// Kernel templates of a per-scheme module (lbm_scheme_<id>.so).
+//
+// The generated translation unit defines, before including this file:
+//   LBM_DIM, LBM_Q, LBM_NCONS, LBM_NPRM, LBM_VMAX, LBM_SHIFTED,
+//   LBM_FOR_EACH_V(X)    X(k, vx, vy, vz) for every population,
+//   lbm_moments / lbm_populations / lbm_relax / lbm_equilibrium_abs /
+//   lbm_relax_abs / lbm_collide  (per-node algebra of the scheme),
+//   lbm_host_shift[], lbm_host_mref[]  (stored shift and its moments),
+//   LBM_STORAGE (double, float, __half or __nv_bfloat16) and LBM_COMPUTE.
+//
+// One thread updates one interior node: it pulls the Q populations
+// f_k(x - v_k) (structure of arrays, so each load of a warp is a contiguous
+// run along the last axis), computes the moments, relaxes them and writes the
+// Q new populations at x.  The two step kernels differ only in where the
+// pulled neighbours come from: ghost layers filled beforehand
+// (k_step_ghost), or the interior wrapped periodically (k_step_periodic).
+#pragma once
+
+#include "lbm_common.cuh"
+
+#include <type_traits>
+
+#ifndef LBM_BLOCK
+#define LBM_BLOCK 128
+#endif
+
+namespace lbm_scheme {
+
+using lbm::Geo;
+using lbm::Store;
+using S = LBM_STORAGE;
+using R = LBM_COMPUTE;
+
+constexpr int kPrm = LBM_NPRM > 0 ? LBM_NPRM : 1;
+
+struct StepArgs {
+  Geo g;
+  long long pull[LBM_Q];  // element offset of the pulled value of population k
+  R prm[kPrm];
+};
+
+struct MomentArgs {
+  Geo g;    // populations
+  Geo gm;   // float64 moments
+  double prm[kPrm];
+};
+
+// interior node handled by this thread, as halo coordinates
+__device__ __forceinline__ bool my_node(const Geo& g, int& i0, int& i1, int& i2) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+#if LBM_DIM == 1
+  if (t >= g.n[0]) return false;
+  i0 = t + g.h[0];
+  i1 = 0;
+  i2 = 0;
+#elif LBM_DIM == 2
+  if (t >= g.n[1]) return false;
+  i0 = blockIdx.y + g.h[0];
+  i1 = t + g.h[1];
+  i2 = 0;
+#else
+  if (t >= g.n[2]) return false;
+  i0 = blockIdx.z + g.h[0];
+  i1 = blockIdx.y + g.h[1];
+  i2 = t + g.h[2];
+#endif
+  return true;
+}
+
+// every node of the halo-extended box (moment transforms)
+__device__ __forceinline__ bool my_cell(const Geo& g, int& i0, int& i1, int& i2) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+#if LBM_DIM == 1
+  if (t >= g.n[0] + 2 * g.h[0]) return false;
+  i0 = t;
+  i1 = 0;
+  i2 = 0;
+#elif LBM_DIM == 2
+  if (t >= g.n[1] + 2 * g.h[1]) return false;
+  i0 = blockIdx.y;
+  i1 = t;
+  i2 = 0;
+#else
+  if (t >= g.n[2] + 2 * g.h[2]) return false;
+  i0 = blockIdx.z;
+  i1 = blockIdx.y;
+  i2 = t;
+#endif
+  return true;
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_step_ghost(const S* __restrict__ f, S* __restrict__ fnew,
+                                                          StepArgs a) {
+  int i0, i1, i2;
+  if (!my_node(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  R g[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) g[k] = (R)Store<S>::load(f + o + a.pull[k]);
+  lbm_collide<R>(g, a.prm);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * a.g.vstride, g[k]);
+}
+
+// offset of the pulled neighbour along one axis, wrapped into the interior
+__device__ __forceinline__ long long wrap_off(int i, int s, int n, int h, long long stride) {
+  int j = i - s;
+  if (j < h) j += n;
+  if (j >= n + h) j -= n;
+  return (long long)(j - i) * stride;
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_step_periodic(const S* __restrict__ f, S* __restrict__ fnew,
+                                                             StepArgs a) {
+  int i0, i1, i2;
+  if (!my_node(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  long long off0[2 * LBM_VMAX + 1], off1[2 * LBM_VMAX + 1], off2[2 * LBM_VMAX + 1];
+#pragma unroll
+  for (int s = -LBM_VMAX; s <= LBM_VMAX; ++s) {
+    off0[s + LBM_VMAX] = LBM_DIM > 0 ? wrap_off(i0, s, a.g.n[0], a.g.h[0], a.g.stride[0]) : 0;
+    off1[s + LBM_VMAX] = LBM_DIM > 1 ? wrap_off(i1, s, a.g.n[1], a.g.h[1], a.g.stride[1]) : 0;
+    off2[s + LBM_VMAX] = LBM_DIM > 2 ? wrap_off(i2, s, a.g.n[2], a.g.h[2], a.g.stride[2]) : 0;
+  }
+  R g[LBM_Q];
+#define LBM_PULL_WRAP(k, vx, vy, vz)                                                            \
+  g[k] = (R)Store<S>::load(f + o + (long long)(k) * a.g.vstride + off0[(vx) + LBM_VMAX] +      \
+                           off1[(vy) + LBM_VMAX] + off2[(vz) + LBM_VMAX]);
+  LBM_FOR_EACH_V(LBM_PULL_WRAP)
+#undef LBM_PULL_WRAP
+  lbm_collide<R>(g, a.prm);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * a.g.vstride, g[k]);
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_transport(const S* __restrict__ f, S* __restrict__ fnew,
+                                                         StepArgs a) {
+  int i0, i1, i2;
+  if (!my_node(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) fnew[o + (long long)k * a.g.vstride] = f[o + a.pull[k]];
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_f2m(const S* __restrict__ f, double* __restrict__ m,
+                                                   MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_cell(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  const long long om = lbm::node_offset(a.gm, i0, i1, i2);
+  double g[LBM_Q], mm[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) g[k] = (double)Store<S>::load(f + o + (long long)k * a.g.vstride);
+  lbm_moments<double>(g, mm);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) m[om + (long long)k * a.gm.vstride] = mm[k] + lbm_dev_mref[k];
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_m2f(const double* __restrict__ m, S* __restrict__ f,
+                                                   MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_cell(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  const long long om = lbm::node_offset(a.gm, i0, i1, i2);
+  double mm[LBM_Q], g[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) mm[k] = m[om + (long long)k * a.gm.vstride];
+  lbm_populations<double>(mm, g);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k)
+    Store<S>::store(f + o + (long long)k * a.g.vstride, (R)(g[k] - lbm_dev_shift[k]));
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_equilibrium(double* __restrict__ m, MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_cell(a.gm, i0, i1, i2)) return;
+  const long long om = lbm::node_offset(a.gm, i0, i1, i2);
+  double mm[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) mm[k] = m[om + (long long)k * a.gm.vstride];
+  lbm_equilibrium_abs<double>(mm, a.prm);
+#pragma unroll
+  for (int k = LBM_NCONS; k < LBM_Q; ++k) m[om + (long long)k * a.gm.vstride] = mm[k];
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_relaxation(double* __restrict__ m, MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_cell(a.gm, i0, i1, i2)) return;
+  const long long om = lbm::node_offset(a.gm, i0, i1, i2);
+  double mm[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) mm[k] = m[om + (long long)k * a.gm.vstride];
+  lbm_relax_abs<double>(mm, a.prm);
+#pragma unroll
+  for (int k = LBM_NCONS; k < LBM_Q; ++k) m[om + (long long)k * a.gm.vstride] = mm[k];
+}
+
+// ------------------------------------------------------------------ host
+inline int check_pop_lattice(const lbm_lattice* lat, const char* who) {
+  int rc = lbm::check_lattice(lat, who);
+  if (rc) return rc;
+  if (lat->dim != LBM_DIM || lat->nv != LBM_Q)
+    return lbm::fail(LBM_ERR_ARG, "%s: lattice dim=%d nv=%d, scheme has dim=%d nv=%d", who, lat->dim,
+                     lat->nv, LBM_DIM, LBM_Q);
+  if (lat->dtype != Store<S>::code)
+    return lbm::fail(LBM_ERR_ARG, "%s: lattice dtype %d, module stores %d", who, lat->dtype, Store<S>::code);
+  for (int d = 0; d < LBM_DIM; ++d)
+    if (lat->halo[d] < LBM_VMAX)
+      return lbm::fail(LBM_ERR_ARG, "%s: halo[%d]=%d below the stencil reach %d", who, d, lat->halo[d], LBM_VMAX);
+  return LBM_OK;
+}
+
+inline int check_moment_lattice(const lbm_lattice* lat, const lbm_lattice* mlat, const char* who) {
+  int rc = lbm::check_lattice(mlat, who);
+  if (rc) return rc;
+  if (mlat->dtype != LBM_F64) return lbm::fail(LBM_ERR_ARG, "%s: moments must be float64", who);
+  if (mlat->dim != LBM_DIM || mlat->nv != LBM_Q) return lbm::fail(LBM_ERR_ARG, "%s: moment lattice shape", who);
+  if (lat) {
+    for (int d = 0; d < 3; ++d)
+      if (lat->n[d] != mlat->n[d] || lat->halo[d] != mlat->halo[d])
+        return lbm::fail(LBM_ERR_ARG, "%s: moment and population lattices differ on axis %d", who, d);
+  }
+  return LBM_OK;
+}
+
+inline dim3 node_grid(const lbm_lattice& l, bool with_halo) {
+  const int L = LBM_DIM - 1;
+  const int e = with_halo ? 2 : 0;
+  unsigned gx = (unsigned)((l.n[L] + e * l.halo[L] + LBM_BLOCK - 1) / LBM_BLOCK);
+  unsigned gy = 1, gz = 1;
+#if LBM_DIM == 2
+  gy = (unsigned)(l.n[0] + e * l.halo[0]);
+#elif LBM_DIM == 3
+  gy = (unsigned)(l.n[1] + e * l.halo[1]);
+  gz = (unsigned)(l.n[0] + e * l.halo[0]);
+#endif
+  return dim3(gx, gy, gz);
+}
+
+inline StepArgs make_step_args(const lbm_lattice& l, const double* prm) {
+  StepArgs a;
+  a.g = lbm::make_geo(l);
+#define LBM_PULL_OFF(k, vx, vy, vz) \
+  a.pull[k] = (long long)(k) * l.vstride - ((long long)(vx) * l.stride[0] + (long long)(vy) * l.stride[1] + (long long)(vz) * l.stride[2]);
+  LBM_FOR_EACH_V(LBM_PULL_OFF)
+#undef LBM_PULL_OFF
+  for (int i = 0; i < kPrm; ++i) a.prm[i] = (i < LBM_NPRM && prm) ? (R)prm[i] : (R)0;
+  return a;
+}
+
+}  // namespace lbm_scheme
+
+extern "C" {
+
+const char* lbm_scheme_last_error(void) { return lbm::error_slot().msg; }
+
+int lbm_scheme_describe(int32_t* nv, int32_t* dim, int32_t* nprm, int32_t* storage, int32_t* compute,
+                        double* shift, double* mref) {
+  if (nv) *nv = LBM_Q;
+  if (dim) *dim = LBM_DIM;
+  if (nprm) *nprm = LBM_NPRM;
+  if (storage) *storage = lbm::Store<lbm_scheme::S>::code;
+  if (compute) *compute = std::is_same<lbm_scheme::R, double>::value ? LBM_F64 : LBM_F32;
+  for (int k = 0; k < LBM_Q; ++k) {
+    if (shift) shift[k] = lbm_host_shift[k];
+    if (mref) mref[k] = lbm_host_mref[k];
+  }
+  return LBM_OK;
+}
+
+static int step_common(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, void* stream,
+                       bool periodic, const char* who) {
+  using namespace lbm_scheme;
+  int rc = check_pop_lattice(lat, who);
+  if (rc) return rc;
+  if (!f || !fnew) return lbm::fail(LBM_ERR_ARG, "%s: NULL populations", who);
+  if (f == fnew) return lbm::fail(LBM_ERR_ARG, "%s: f and fnew must be distinct buffers", who);
+  if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "%s: %d parameters expected", who, LBM_NPRM);
+  StepArgs a = make_step_args(*lat, prm);
+  dim3 grid = node_grid(*lat, false);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (periodic)
+    k_step_periodic<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a);
+  else
+    k_step_ghost<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a);
+  return lbm::launch_check(who);
+}
+
+int lbm_one_time_step(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, void* stream) {
+  return step_common(f, fnew, lat, prm, stream, false, "lbm_one_time_step");
+}
+
+int lbm_one_time_step_periodic(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                               void* stream) {
+  return step_common(f, fnew, lat, prm, stream, true, "lbm_one_time_step_periodic");
+}
+
+int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_pop_lattice(lat, "lbm_transport");
+  if (rc) return rc;
+  if (!f || !fnew || f == fnew) return lbm::fail(LBM_ERR_ARG, "lbm_transport: bad buffers");
+  StepArgs a = make_step_args(*lat, nullptr);
+  k_transport<<<node_grid(*lat, false), LBM_BLOCK, 0, (cudaStream_t)stream>>>((const S*)f, (S*)fnew, a);
+  return lbm::launch_check("lbm_transport");
+}
+
+static lbm_scheme::MomentArgs make_moment_args(const lbm_lattice* lat, const lbm_lattice* mlat, const double* prm) {
+  lbm_scheme::MomentArgs a;
+  a.g = lbm::make_geo(lat ? *lat : *mlat);
+  a.gm = lbm::make_geo(*mlat);
+  for (int i = 0; i < lbm_scheme::kPrm; ++i) a.prm[i] = (i < LBM_NPRM && prm) ? prm[i] : 0.0;
+  return a;
+}
+
+int lbm_f2m(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_pop_lattice(lat, "lbm_f2m");
+  if (!rc) rc = check_moment_lattice(lat, mlat, "lbm_f2m");
+  if (rc) return rc;
+  if (!f || !m) return lbm::fail(LBM_ERR_ARG, "lbm_f2m: NULL buffer");
+  MomentArgs a = make_moment_args(lat, mlat, nullptr);
+  k_f2m<<<node_grid(*lat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>((const S*)f, m, a);
+  return lbm::launch_check("lbm_f2m");
+}
+
+int lbm_m2f(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_pop_lattice(lat, "lbm_m2f");
+  if (!rc) rc = check_moment_lattice(lat, mlat, "lbm_m2f");
+  if (rc) return rc;
+  if (!f || !m) return lbm::fail(LBM_ERR_ARG, "lbm_m2f: NULL buffer");
+  MomentArgs a = make_moment_args(lat, mlat, nullptr);
+  k_m2f<<<node_grid(*lat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, (S*)f, a);
+  return lbm::launch_check("lbm_m2f");
+}
+
+int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_moment_lattice(nullptr, mlat, "lbm_equilibrium");
+  if (rc) return rc;
+  if (!m) return lbm::fail(LBM_ERR_ARG, "lbm_equilibrium: NULL buffer");
+  if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "lbm_equilibrium: parameters expected");
+  MomentArgs a = make_moment_args(nullptr, mlat, prm);
+  k_equilibrium<<<node_grid(*mlat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, a);
+  return lbm::launch_check("lbm_equilibrium");
+}
+
+int lbm_relaxation(double* m, const lbm_lattice* mlat, const double* prm, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_moment_lattice(nullptr, mlat, "lbm_relaxation");
+  if (rc) return rc;
+  if (!m) return lbm::fail(LBM_ERR_ARG, "lbm_relaxation: NULL buffer");
+  if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "lbm_relaxation: parameters expected");
+  MomentArgs a = make_moment_args(nullptr, mlat, prm);
+  k_relaxation<<<node_grid(*mlat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, a);
+  return lbm::launch_check("lbm_relaxation");
+}
+
+}  // extern "C"

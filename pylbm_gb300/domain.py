@@ -1,0 +1,170 @@
+"""Halo-extended lattice, fluid/solid map and per-link wall distances/labels.
+
+Same contract as pylbm's ``Domain`` (pylbm/domain.py:87): nodes are cell
+centres ``xmin + (i + 1/2) dx`` plus ``vmax`` ghost layers per side
+(``create_coords`` :385-442); ``in_or_out`` is 999 in the fluid and -1 in
+the solid/ghost layers; ``distance[k, node]`` is the fraction of the link
+``node -> node + v_k`` before a wall and ``flag[k, node]`` that wall's label,
+999 elsewhere.  Box walls are applied axis by axis with a strict
+"only if shorter" rule (:463-521), obstacles after them (:523-620), then
+flags on solid nodes are cleared (``clean``).  The boundary link lists built
+from these arrays decide which populations the boundary kernels write, so
+the rules (including their tie-breaking) are kept identical.
+"""
+import numpy as np
+
+from .stencil import Stencil
+from .scheme import _box_dim
+
+VALIN = 999
+VALOUT = -1
+
+
+class Domain:
+    def __init__(self, dico, stencil=None):
+        self.valin = VALIN
+        self.valout = VALOUT
+        self.dim = _box_dim(dico)
+        box = dico["box"]
+        bounds = [box["x"]]
+        if self.dim > 1:
+            bounds.append(box["y"])
+        if self.dim > 2:
+            bounds.append(box["z"])
+        self.bounds = np.asarray(bounds, dtype=np.float64)
+        lab = box.get("label", -1)
+        if isinstance(lab, (int, np.integer)):
+            lab = [int(lab)] * (2 * self.dim)
+        lab = list(lab)
+        if len(lab) != 2 * self.dim:
+            raise ValueError("the box label list must have 2*dim entries")
+        self.box_label = lab
+        self.dx = float(dico["space_step"])
+        self.stencil = stencil if stencil is not None else Stencil.from_dico(dico, self.dim)
+        self.elements = list(dico.get("elements", []) or [])
+        for e in self.elements:
+            if getattr(e, "dim", self.dim) != self.dim:
+                raise ValueError("element and box dimensions differ")
+
+        self.global_size = []
+        for k in range(self.dim):
+            n = (self.bounds[k][1] - self.bounds[k][0]) / self.dx
+            if not float(n).is_integer():
+                r = round(n)
+                if abs(r - n) < self.dx:
+                    n = r
+                else:
+                    raise ValueError(f"box length along axis {k} is not a multiple of the space step")
+            self.global_size.append(int(n))
+        self.halo = np.asarray(self.stencil.vmax, dtype=np.int64)
+        if np.any(self.halo < 1):
+            raise ValueError("every axis needs at least one non-zero velocity component")
+        self.coords_halo = []
+        for k in range(self.dim):
+            h = int(self.halo[k])
+            beg = self.dx * (h - 0.5)
+            self.coords_halo.append(np.linspace(self.bounds[k][0] - beg, self.bounds[k][1] + beg,
+                                                self.global_size[k] + 2 * h))
+        self.coords = [c[int(h):-int(h)] for c, h in zip(self.coords_halo, self.halo)]
+
+        uv = self.stencil.unique_v
+        nu = uv.shape[0]
+        shape = self.shape_halo
+        self.in_or_out = np.full(shape, float(VALOUT))
+        inner = tuple(slice(int(h), -int(h)) for h in self.halo)
+        self.in_or_out[inner] = VALIN
+        self.distance = np.full([nu] + shape, float(VALIN))
+        self.flag = np.full([nu] + shape, VALIN, dtype=np.int64)
+        self._add_box(inner)
+        for e in self.elements:
+            self._add_element(e)
+        self._clean()
+
+    @property
+    def shape_halo(self):
+        return [int(c.size) for c in self.coords_halo]
+
+    @property
+    def shape_in(self):
+        return [int(c.size) for c in self.coords]
+
+    def list_of_labels(self):
+        labs = np.unique(self.box_label)
+        elabs = [l for e in self.elements for l in e.label]
+        return np.union1d(labs, np.asarray(elabs, dtype=labs.dtype)) if elabs else labs
+
+    def _add_box(self, inner):
+        uv = self.stencil.unique_v
+        dist = self.distance[(slice(None),) + inner]
+        flag = self.flag[(slice(None),) + inner]
+        for axis in range(self.dim):
+            for k in range(uv.shape[0]):
+                c = int(uv[k, axis])
+                if c < 0 and self.box_label[2 * axis] != -2:
+                    rows, lab = [(i, (i + 0.5) / -c) for i in range(-c)], self.box_label[2 * axis]
+                elif c > 0 and self.box_label[2 * axis + 1] != -2:
+                    rows, lab = [(-i - 1, (i + 0.5) / c) for i in range(c)], self.box_label[2 * axis + 1]
+                else:
+                    continue
+                for row, d in rows:
+                    sl = [slice(None)] * self.dim
+                    sl[axis] = row
+                    dv = dist[k][tuple(sl)]
+                    fv = flag[k][tuple(sl)]
+                    upd = dv > d
+                    dv[upd] = d
+                    fv[upd] = lab
+
+    def _add_element(self, elem):
+        vmax = self.halo
+        lo, hi = elem.get_bounds()
+        origin = np.array([c[0] for c in self.coords_halo])
+        nmin = np.maximum(vmax, np.array((lo - origin) / self.dx, int) - vmax)
+        nmax = np.minimum(vmax + np.asarray(self.shape_in), np.array((hi - origin) / self.dx, int) + vmax + 1)
+        region = tuple(slice(a, b) for a, b in zip(nmin, nmax))
+        ioo = self.in_or_out[region]
+        grid = np.meshgrid(*(self.coords_halo[d][region[d]] for d in range(self.dim)),
+                           sparse=True, indexing="ij")
+        if not elem.isfluid:
+            solid = elem.point_inside(grid)
+            fluid = np.logical_not(solid)
+            ioo[solid] = VALOUT
+        else:
+            fluid = elem.point_inside(grid)
+            solid = np.logical_not(fluid)
+            ioo[fluid] = VALIN
+        uv = self.stencil.unique_v
+        for k in range(uv.shape[0]):
+            vk = uv[k]
+            if not np.any(vk != 0):
+                continue
+            shifted = tuple(slice(a + vk[d], b + vk[d]) for d, (a, b) in enumerate(zip(nmin, nmax)))
+            out_cells = self.in_or_out[shifted] == VALOUT
+            alpha, border = elem.distance(grid, self.dx * vk, 1.0)
+            sel = np.logical_and(alpha > 0, fluid)
+            if out_cells.size:
+                sel = np.logical_and(sel, out_cells)
+            dk = self.distance[k][region]
+            fk = self.flag[k][region]
+            if elem.isfluid:
+                back = np.logical_and(np.logical_not(out_cells), ioo == VALIN)
+                dk[back] = VALIN
+                fk[back] = VALIN
+            else:
+                dk[solid] = VALIN
+                fk[solid] = VALIN
+            idx = np.where(sel)
+            if not elem.isfluid:
+                keep = alpha[idx] < dk[idx]
+            else:
+                keep = np.logical_or(alpha[idx] > dk[idx], dk[idx] == VALIN)
+            idx = tuple(i[keep] for i in idx)
+            dk[idx] = alpha[idx]
+            fk[idx] = border[idx]
+
+    def _clean(self):
+        solid = self.in_or_out == VALOUT
+        for k in range(self.distance.shape[0]):
+            sel = np.logical_and(self.distance[k] > 0, solid)
+            self.distance[k][sel] = VALIN
+            self.flag[k][sel] = VALIN

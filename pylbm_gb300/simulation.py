@@ -1,0 +1,398 @@
+"""``Simulation`` with ``generator='cuda'``: pylbm's time loop on one GB300.
+
+The public surface follows pylbm/simulation.py:33: ``Simulation(dico, sorder,
+dtype, check_inverse, initialize)``, ``one_time_step()`` (:393-420),
+``boundary_condition()`` (:374-390), ``m[...]``/``F[...]`` item access
+(:216-256), ``t``, ``nt``, ``dt``, ``extra_parameters``.  The populations live
+on the device in the padded structure-of-arrays layout of the C ABI; a step is
+
+    lbm_update_halo(F)                       periodic ghost refresh
+    lbm_<method>(F, iload0, istore, rhs)     every boundary method in order
+    lbm_one_time_step(F, Fnew)               fused pull-stream + collide
+    swap(F, Fnew)
+
+and a domain that is periodic along every axis skips the first two and uses
+``lbm_one_time_step_periodic``, which wraps the pull inside the interior.
+
+``dtype`` selects the storage type: "float64" (FP64 storage and arithmetic,
+the parity path) or "float32"/"float16"/"bfloat16" (values stored as
+deviations f - feq(c0) from the equilibrium of a reference state c0 of the
+conserved moments, arithmetic in FP32).
+"""
+import ctypes
+import types
+
+import numpy as np
+import sympy as sp
+
+from . import runtime
+from .boundary import Boundary
+from .codegen import SchemeSource
+from .domain import Domain
+from .scheme import Scheme
+
+_STORAGES = ("float64", "float32", "float16", "bfloat16")
+
+
+class _ItemAccess:
+    """``sim.m[key]`` / ``sim.m[key] = value`` helper (pylbm/utils.py:26-81)."""
+
+    def __init__(self, getter, setter=None):
+        self._get = getter
+        self._set = setter
+
+    def __getitem__(self, key):
+        return self._get(key)
+
+    def __setitem__(self, key, value):
+        if self._set is None:
+            raise AttributeError("read-only item access")
+        self._set(key, value)
+
+
+def _round_reference(values):
+    """Reference value of a conserved moment: its mean, to 4 significant digits."""
+    mean = float(np.mean(values))
+    scale = float(np.max(np.abs(values))) if values.size else 0.0
+    if scale == 0.0 or abs(mean) <= 1e-6 * scale:
+        return 0.0
+    return float(f"{mean:.4g}")
+
+
+def _to_storage(host, dtype):
+    """float64 numpy -> raw storage array of ``dtype``."""
+    if dtype == "float64":
+        return np.ascontiguousarray(host, dtype=np.float64)
+    if dtype == "float32":
+        return np.ascontiguousarray(host, dtype=np.float32)
+    if dtype == "float16":
+        return np.ascontiguousarray(host, dtype=np.float16)
+    # bfloat16: round-to-nearest-even on the float32 bit pattern
+    b = np.ascontiguousarray(host, dtype=np.float32).view(np.uint32)
+    rounding = ((b >> 16) & 1) + 0x7FFF
+    return ((b + rounding) >> 16).astype(np.uint16)
+
+
+def _from_storage(raw, dtype):
+    if dtype == "bfloat16":
+        return (raw.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    return raw.astype(np.float64)
+
+
+_RAW = {"float64": np.float64, "float32": np.float32, "float16": np.float16, "bfloat16": np.uint16}
+
+
+class Simulation:
+    """A pylbm simulation whose hot path runs on the GPU.
+
+    Parameters
+    ----------
+    dico : dict
+        pylbm scheme dictionary; ``generator`` must be 'cuda' (or absent).
+    sorder : ignored
+        kept for signature compatibility: the device layout is fixed.
+    dtype : str
+        storage type, one of "float64", "float32", "float16", "bfloat16".
+    initialize : bool
+        initialise the populations now (else on the first step).
+    shifted : bool or None
+        store deviations from feq(c0); default: every type but float64.
+    """
+
+    def __init__(self, dico, sorder=None, dtype="float64", check_inverse=False, initialize=True,
+                 shifted=None):
+        gen = str(dico.get("generator", "cuda")).upper()
+        if gen != "CUDA":
+            raise ValueError(f"pylbm_gb300 implements generator='cuda', not {gen!r}")
+        if dtype not in _STORAGES:
+            raise ValueError(f"dtype must be one of {_STORAGES}")
+        self.dico = dico
+        self.scheme = Scheme(dico)
+        self.domain = Domain(dico, self.scheme.stencil)
+        if self.domain.dim != self.scheme.dim:
+            raise ValueError("the dimension of the domain and of the scheme are not the same")
+        self.dim = self.domain.dim
+        self.storage = dtype
+        self.compute = "float64" if dtype == "float64" else "float32"
+        self.shifted = (dtype != "float64") if shifted is None else bool(shifted)
+        self.t = 0.0
+        self.nt = 0
+        self._dt = self.domain.dx / self.scheme.la_float
+        self.extra_parameters = {}
+        self.init_type = dico.get("inittype", "moments")
+        self.init_data = dico.get("init", None)
+        self.periodic = all(l == -1 for l in self.domain.box_label) and not self.domain.elements
+
+        self.bc = Boundary(self.domain, dico)
+        for meth in self.bc.methods:
+            meth.set_iload()
+
+        self._core = runtime.core()
+        shape_in = self.domain.shape_in
+        halo = [int(h) for h in self.domain.halo]
+        self._lat = runtime.lattice(self.dim, self.scheme.nv, dtype, shape_in, halo)
+        self._mlat = runtime.lattice(self.dim, self.scheme.nv, "float64", shape_in, halo)
+        es = runtime.DTYPE_SIZE[dtype]
+        self._F = runtime.DeviceBuffer(self._lat.elements * es)
+        self._Fnew = runtime.DeviceBuffer(self._lat.elements * es)
+        self._M = None
+        self._stream = None
+        self.module = None
+        self._m_cache = {}
+        self._update_m = True
+        self._bc_dev = []
+        self._need_init = True
+        if initialize:
+            self._initialize()
+
+    # ------------------------------------------------------------------ setup
+    @property
+    def dt(self):
+        return self._dt
+
+    def extra_parameters_str(self):
+        return {str(k): v for k, v in self.extra_parameters.items()}
+
+    def _prm(self):
+        vals = self.extra_parameters_str()
+        names = [str(s) for s in self.scheme.free_symbols]
+        missing = [n for n in names if n not in vals]
+        if missing:
+            raise ValueError(f"extra_parameters must give values for {missing}")
+        arr = np.array([float(vals[n]) for n in names] + [0.0], dtype=np.float64)
+        return arr
+
+    def _mbuf(self):
+        if self._M is None:
+            self._M = runtime.DeviceBuffer(self._mlat.elements * 8)
+        return self._M
+
+    def _halo_view(self, flat, lat, nv=None):
+        """View of a downloaded padded buffer as (nv, *shape_halo)."""
+        nv = lat.nv if nv is None else nv
+        shape = [nv] + self.domain.shape_halo
+        strides_el = [lat.vstride] + [lat.stride[d] for d in range(self.dim)]
+        es = flat.itemsize
+        return np.lib.stride_tricks.as_strided(flat[lat.origin:], shape=shape,
+                                               strides=[s * es for s in strides_el])
+
+    def _padded(self, arr, lat, dtype):
+        """Pack (nv, *shape_halo) values into a padded flat buffer of ``lat``."""
+        flat = np.zeros(lat.elements, dtype=dtype)
+        view = self._halo_view(flat, lat, arr.shape[0])
+        view[...] = arr
+        return flat
+
+    def _initialize(self):
+        sc = self.scheme
+        nv = sc.nv
+        coords = np.meshgrid(*self.domain.coords_halo, sparse=True, indexing="ij")
+        shape = self.domain.shape_halo
+        if self.init_type not in ("moments", "distributions"):
+            raise ValueError("inittype must be 'moments' or 'distributions'")
+        # only the conserved moments are given for a moment initialisation;
+        # the device computes the others (equilibrium) and the populations
+        nplanes = sc.nconsm if self.init_type == "moments" else nv
+        arr = np.zeros([nplanes] + shape)
+        if self.init_data is not None:
+            for key, val in self.init_data.items():
+                if self.init_type == "moments":
+                    idx = sc.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
+                else:
+                    idx = int(key)
+                if idx >= nplanes:
+                    raise ValueError(f"initial value given for non-conserved moment {key}")
+                if isinstance(val, tuple):
+                    fargs = tuple(coords) + (tuple(val[1]) if len(val) == 2 else ())
+                    arr[idx] = val[0](*fargs)
+                elif isinstance(val, types.FunctionType):
+                    arr[idx] = val(*coords)
+                else:
+                    arr[idx] = val
+        if self.init_type == "distributions":
+            arr = np.einsum("ij,j...->i...", sc.M, arr)
+        inner = tuple(slice(int(h), -int(h)) for h in self.domain.halo)
+        c0 = [_round_reference(arr[c][inner]) for c in range(sc.nconsm)] if self.shifted else None
+        src = SchemeSource(sc, self.shifted, c0)
+        self.module = runtime.SchemeModule(src, self.storage, self.compute)
+        for k in range(nv):
+            self._lat.shift[k] = float(self.module.shift[k])
+        mbuf = self._mbuf()
+        plane = np.zeros(self._mlat.vstride, dtype=np.float64)
+        for c in range(nplanes):
+            self._plane_view(plane, self._mlat)[...] = arr[c]
+            mbuf.upload(plane, offset=c * self._mlat.vstride * 8)
+        del arr
+        prm = self._prm()
+        pp = prm.ctypes.data_as(ctypes.c_void_p)
+        if self.init_type == "moments":
+            self.module.call(self.module.lib.lbm_equilibrium(mbuf.handle, ctypes.byref(self._mlat), pp, None))
+        self.module.call(self.module.lib.lbm_m2f(mbuf.handle, ctypes.byref(self._mlat), self._F.handle,
+                                                 ctypes.byref(self._lat), None))
+        runtime.check(self._core.lbm_memcpy(self._Fnew.handle, self._F.handle, self._F.nbytes, runtime.D2D, None))
+        runtime.check(self._core.lbm_stream_synchronize(None))
+        for meth in self.bc.methods:
+            meth.prepare_rhs(self)
+            meth.fix_iload()
+            meth.set_rhs()
+        self._upload_bc()
+        self._update_m = True
+        self._m_cache = {}
+        self._need_init = False
+
+    def _upload_bc(self):
+        self._bc_dev = []
+        for meth in self.bc.methods:
+            il = runtime.DeviceBuffer(max(meth.iload[0].nbytes, 4))
+            il.upload(meth.iload[0])
+            st = runtime.DeviceBuffer(max(meth.istore.nbytes, 4))
+            st.upload(meth.istore)
+            rhs = runtime.DeviceBuffer(max(meth.rhs.nbytes, 8))
+            rhs.upload(meth.rhs)
+            ordered = 0 if self._links_independent(meth) else 1
+            self._bc_dev.append((meth, il, st, rhs, ordered))
+
+    @staticmethod
+    def _links_independent(meth):
+        """True when no link reads a slot another link of the method writes."""
+        st = {tuple(r) for r in meth.istore.tolist()}
+        return not any(tuple(r) in st for r in meth.iload[0].tolist())
+
+    # ------------------------------------------------------------------ step
+    def boundary_condition(self):
+        """Ghost refresh then every boundary method (pylbm/simulation.py:374-390)."""
+        if self.periodic:
+            return
+        lat = ctypes.byref(self._lat)
+        runtime.check(self._core.lbm_update_halo(self._F.handle, lat, self._stream))
+        for meth, il, st, rhs, ordered in self._bc_dev:
+            if meth.update_feq(self):
+                meth.set_rhs()
+                rhs.upload(meth.rhs)
+            if meth.kind == "bounce_back":
+                rc = self._core.lbm_bounce_back(self._F.handle, il.handle, st.handle, meth.ncond, rhs.handle, lat,
+                                                ordered, self._stream)
+            elif meth.kind == "anti_bounce_back":
+                rc = self._core.lbm_anti_bounce_back(self._F.handle, il.handle, st.handle, meth.ncond, rhs.handle,
+                                                     lat, ordered, self._stream)
+            else:
+                rc = self._core.lbm_neumann(self._F.handle, il.handle, st.handle, meth.ncond, lat, ordered,
+                                            self._stream)
+            runtime.check(rc)
+
+    def one_time_step(self):
+        """One time step (pylbm/simulation.py:393-420)."""
+        if self._need_init:
+            self._initialize()
+        self._update_m = True
+        self._m_cache = {}
+        self.boundary_condition()
+        prm = self._prm()
+        pp = prm.ctypes.data_as(ctypes.c_void_p)
+        fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
+        self.module.call(fn(self._F.handle, self._Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
+        self._F, self._Fnew = self._Fnew, self._F
+        self.t += self.dt
+        self.nt += 1
+
+    def run(self, nsteps):
+        for _ in range(int(nsteps)):
+            self.one_time_step()
+
+    def synchronize(self):
+        runtime.check(self._core.lbm_stream_synchronize(self._stream))
+
+    # ------------------------------------------------------------------ access
+    def _moment_halo(self, key):
+        idx = self.scheme.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
+        if self._update_m:
+            self._m_cache = {}
+            mbuf = self._mbuf()
+            self.module.call(self.module.lib.lbm_f2m(self._F.handle, ctypes.byref(self._lat), mbuf.handle,
+                                                     ctypes.byref(self._mlat), None))
+            self._update_m = False
+        if idx not in self._m_cache:
+            plane = np.empty(self._mlat.vstride, dtype=np.float64)
+            self._mbuf().download(plane, offset=idx * self._mlat.vstride * 8)
+            view = self._plane_view(plane, self._mlat)
+            self._m_cache[idx] = np.array(view)
+        return self._m_cache[idx]
+
+    def _plane_view(self, plane, lat):
+        shape = self.domain.shape_halo
+        es = plane.itemsize
+        return np.lib.stride_tricks.as_strided(plane[lat.origin:], shape=shape,
+                                               strides=[lat.stride[d] * es for d in range(self.dim)])
+
+    def _inner(self):
+        return tuple(slice(int(h), -int(h)) for h in self.domain.halo)
+
+    @property
+    def m_halo(self):
+        return _ItemAccess(self._moment_halo)
+
+    @property
+    def m(self):
+        """Moments on the interior nodes (pylbm/simulation.py:216-224)."""
+        return _ItemAccess(lambda key: self._moment_halo(key)[self._inner()])
+
+    def _population_halo(self, k):
+        k = int(k)
+        es = runtime.DTYPE_SIZE[self.storage]
+        raw = np.empty(self._lat.vstride, dtype=_RAW[self.storage])
+        self._F.download(raw, offset=k * self._lat.vstride * es)
+        vals = _from_storage(raw, self.storage)
+        return np.array(self._plane_view(vals, self._lat)) + float(self._lat.shift[k])
+
+    def _set_population_halo(self, k, value):
+        k = int(k)
+        cur = self._population_halo(k)
+        cur[...] = value
+        es = runtime.DTYPE_SIZE[self.storage]
+        plane = np.zeros(self._lat.vstride, dtype=np.float64)
+        self._plane_view(plane, self._lat)[...] = cur - float(self._lat.shift[k])
+        self._F.upload(_to_storage(plane, self.storage), offset=k * self._lat.vstride * es)
+        self._update_m = True
+        self._m_cache = {}
+
+    @property
+    def F_halo(self):
+        return _ItemAccess(self._population_halo, self._set_population_halo)
+
+    @property
+    def F(self):
+        """Populations on the interior nodes (pylbm/simulation.py:248-256)."""
+        return _ItemAccess(lambda k: self._population_halo(k)[self._inner()])
+
+    # ------------------------------------------------------------------ checks
+    def population_sums(self):
+        """FP64 sum of every population over the interior, and the NaN/Inf count."""
+        size = ctypes.c_size_t()
+        runtime.check(self._core.lbm_population_sums_scratch_bytes(ctypes.byref(self._lat), ctypes.byref(size)))
+        scratch = runtime.DeviceBuffer(size.value)
+        out = runtime.DeviceBuffer(8 * self.scheme.nv + 8)
+        runtime.check(self._core.lbm_population_sums(self._F.handle, ctypes.byref(self._lat), out.handle,
+                                                     ctypes.c_void_p(out.ptr + 8 * self.scheme.nv), scratch.handle,
+                                                     size.value, self._stream))
+        host = np.empty(self.scheme.nv + 1, dtype=np.float64)
+        out.download(host, stream=self._stream)
+        sums = host[:self.scheme.nv]
+        bad = int(np.frombuffer(host[self.scheme.nv:].tobytes()[:4], dtype=np.int32)[0])
+        return sums, bad
+
+    def conserved_sums(self):
+        """FP64 totals of the conserved moments (mass, momentum, ...)."""
+        sums, bad = self.population_sums()
+        if bad:
+            raise FloatingPointError(f"non-finite populations detected ({bad} blocks)")
+        return self.scheme.M[:self.scheme.nconsm] @ sums
+
+    def free(self):
+        for b in (self._F, self._Fnew, self._M):
+            if b is not None:
+                b.free()
+        for _, il, st, rhs, _o in self._bc_dev:
+            il.free()
+            st.free()
+            rhs.free()
+        self._bc_dev = []

@@ -1,0 +1,166 @@
+"""Host-side logic against the reference (golden fixtures), and the C ABI build.
+
+No GPU needed: velocity numbering, moment matrices, domain flags and boundary
+lists must equal pylbm's exactly; the libraries must build for sm_103a and
+export every entry point of include/lbm_gb300.h.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+from pylbm_gb300 import runtime
+from pylbm_gb300 import workloads as W
+from pylbm_gb300.boundary import Boundary
+from pylbm_gb300.codegen import SchemeSource
+from pylbm_gb300.domain import Domain
+from pylbm_gb300.scheme import Scheme, SchemeError
+from pylbm_gb300.stencil import velocity, velocity_number
+
+
+def test_velocity_numbering_matches_reference():
+    g = golden("velocities.npz")
+    for dim in (1, 2, 3):
+        ref = g[f"v{dim}"]
+        ours = np.array([velocity(dim, i) for i in range(ref.shape[0])])
+        assert np.array_equal(ours, ref.reshape(ours.shape))
+        for i in range(ref.shape[0]):
+            assert velocity_number(ours[i]) == i
+
+
+@pytest.mark.parametrize("fixture,dico", [
+    ("cavity_n32.npz", lambda: W.cavity(n=32)),
+    ("tgv3d_n16.npz", lambda: W.tgv3d(n=16)),
+])
+def test_moment_matrices_match_reference(fixture, dico):
+    g = golden(fixture)
+    sc = Scheme(dico())
+    assert np.array_equal(sc.M, g["M"])
+    assert np.abs(sc.invM - g["invM"]).max() < 1e-15
+    assert [str(c) for c in sc.consm] == list(g["consm"])
+    assert np.allclose(sc.rates_numpy(), g["s"], rtol=0, atol=1e-14)
+
+
+def _bc_equal(methods, g):
+    assert len(methods) == int(g["bc_count"])
+    for i, meth in enumerate(methods):
+        assert type(meth).__name__ == str(g[f"bc{i}_name"])
+        assert np.array_equal(meth.istore, g[f"bc{i}_istore"])
+        assert np.array_equal(meth.iload[0], g[f"bc{i}_iload0"])
+
+
+class _HostSim:
+    """Just enough of a simulation for prepare_rhs on the host."""
+
+    def __init__(self, dico):
+        self.scheme = Scheme(dico)
+        self.domain = Domain(dico, self.scheme.stencil)
+        self.extra_parameters = {}
+
+    def extra_parameters_str(self):
+        return {}
+
+
+@pytest.mark.parametrize("fixture,dico", [
+    ("cavity_n32.npz", lambda: W.cavity(n=32)),
+    ("cylinder_small.npz", lambda: W.cylinder(nx=96, ny=32, radius=5, center=(24, 17), re=40.0)),
+])
+def test_boundary_lists_match_reference(fixture, dico):
+    g = golden(fixture)
+    d = dico()
+    sim = _HostSim(d)
+    bc = Boundary(sim.domain, d)
+    for meth in bc.methods:
+        meth.set_iload()
+        meth.prepare_rhs(sim)
+        meth.fix_iload()
+        meth.set_rhs()
+    _bc_equal(bc.methods, g)
+    for i, meth in enumerate(bc.methods):
+        assert np.abs(meth.rhs - g[f"bc{i}_rhs"]).max() < 1e-15
+
+
+def test_domain_flags_match_reference():
+    g = golden("cylinder_small.npz")
+    d = W.cylinder(nx=96, ny=32, radius=5, center=(24, 17), re=40.0)
+    dom = Domain(d)
+    assert np.array_equal(dom.flag, g["flag"])
+    assert np.array_equal(dom.in_or_out, g["in_or_out"])
+    assert np.abs(dom.distance - g["distance"]).max() < 1e-14
+
+
+def test_unsupported_scheme_is_rejected():
+    d = W.cavity(n=8)
+    d["relative_velocity"] = [W.QX / W.RHO, W.QY / W.RHO]
+    with pytest.raises(SchemeError):
+        Scheme(d)
+
+
+def test_shifted_source_cancels_reference_state():
+    """The generated deviation equilibrium has no constant term."""
+    sc = Scheme(W.cavity(n=8))
+    src = SchemeSource(sc, shifted=True, c0=[1, 0, 0])
+    assert np.allclose(src.shift_float, [4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+    text = src.header()
+    assert "lbm_relax" in text and "LBM_FOR_EACH_V" in text
+
+
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "lbm_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\**(lbm_\w+)\s*\(", text, flags=re.M)
+
+
+def test_core_library_builds_and_exports_header():
+    path = runtime.build_core()
+    lib = ctypes.CDLL(path)
+    names = _declared_symbols()
+    core_names = [n for n in names if not n.startswith("lbm_scheme") and n not in runtime_scheme_symbols()]
+    assert core_names
+    for n in core_names:
+        assert hasattr(lib, n), n
+
+
+def runtime_scheme_symbols():
+    return {"lbm_one_time_step", "lbm_one_time_step_periodic", "lbm_transport", "lbm_f2m", "lbm_m2f",
+            "lbm_equilibrium", "lbm_relaxation", "lbm_scheme_last_error", "lbm_scheme_describe"}
+
+
+def test_scheme_module_builds_and_exports_header():
+    sc = Scheme(W.cavity(n=8))
+    mod = runtime.SchemeModule(SchemeSource(sc, shifted=False), "float64", "float64")
+    declared = set(_declared_symbols())
+    for n in runtime_scheme_symbols():
+        assert n in declared
+        assert hasattr(mod.lib, n), n
+    assert mod.nv == 9 and mod.dim == 2
+
+
+def test_lattice_layout():
+    lat = runtime.lattice(2, 9, "float32", [256, 256], [1, 1])
+    assert lat.stride[1] == 1
+    assert lat.stride[0] % 8 == 0                    # 32-byte rows
+    assert (lat.origin + 1) * 4 % 32 == 0            # interior rows start aligned
+    assert lat.vstride * 4 % 128 == 0
+    assert lat.elements == 9 * lat.vstride
+    lat3 = runtime.lattice(3, 19, "float16", [16, 8, 4], [1, 1, 1])
+    assert lat3.stride[2] == 1 and lat3.stride[1] % 16 == 0
+    assert lat3.stride[0] == lat3.stride[1] * (8 + 2)
+
+
+def test_c_abi_rejects_bad_arguments_without_gpu():
+    lib = runtime.core()
+    lat = runtime.Lattice()
+    rc = lib.lbm_lattice_init(ctypes.byref(lat), 4, 9, 0, None, None)
+    assert rc == 1
+    assert b"NULL" in lib.lbm_last_error() or b"dim" in lib.lbm_last_error()
+    n3 = (ctypes.c_int32 * 3)(8, 8, 1)
+    h3 = (ctypes.c_int32 * 3)(1, 1, 0)
+    assert lib.lbm_lattice_init(ctypes.byref(lat), 2, 9, 7, ctypes.cast(n3, ctypes.c_void_p),
+                                ctypes.cast(h3, ctypes.c_void_p)) == 1
+    good = runtime.lattice(2, 9, "float64", [8, 8], [1, 1])
+    good.n[0] = 0
+    assert lib.lbm_update_halo(None, ctypes.byref(good), None) == 1

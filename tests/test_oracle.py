@@ -1,0 +1,80 @@
+"""The CPU oracle against the reference's own outputs (golden fixtures).
+
+The fixtures were produced by running pylbm 0.11.0's Cython generator on the
+same dictionaries (tests/golden/make_golden.py).  The bound here is the
+oracle's, not the GPU's: the oracle evaluates M f and M^-1 m in full float64
+where the reference's generated code rounds its constants to the printed
+decimal digits, which leaves ~1e-12 after a few hundred steps.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+from oracle import OracleSimulation, equilibrium_table
+from pylbm_gb300 import workloads as W
+
+
+def test_cavity_n32_against_reference():
+    g = golden("cavity_n32.npz")
+    o = OracleSimulation(W.cavity(n=32))
+    o.initialize()
+    assert rel_err(o.moments(), g["m0"]).max() < 1e-14
+    o.run(50)
+    assert rel_err(o.moments(), g["m50"]).max() < 1e-12
+    o.run(250)
+    assert rel_err(o.moments(), g["m300"]).max() < 2e-12
+
+
+def test_cylinder_against_reference():
+    g = golden("cylinder_small.npz")
+    o = OracleSimulation(W.cylinder(nx=96, ny=32, radius=5, center=(24, 17), re=40.0))
+    o.run(100)
+    assert rel_err(o.moments(), g["m100"]).max() < 5e-12
+
+
+def test_tgv3d_against_reference():
+    g = golden("tgv3d_n16.npz")
+    o = OracleSimulation(W.tgv3d(n=16))
+    o.initialize()
+    assert rel_err(o.moments(), g["m0"]).max() < 1e-12
+    o.run(20)
+    assert rel_err(o.moments(), g["m20"]).max() < 5e-12
+
+
+def test_shear_layer_against_reference():
+    g = golden("shear_n64.npz")
+    o = OracleSimulation(W.shear_layer(n=64))
+    o.initialize()
+    assert rel_err(o.moments(), g["m0"]).max() < 1e-12
+    o.run(200)
+    assert rel_err(o.moments(), g["m200"]).max() < 5e-12
+
+
+def test_cavity_full_size_sampled():
+    """The 256^2 x 1000-step cavity of the reference, at every 4th node and the edges."""
+    g = golden("cavity_n256_sampled.npz")
+    o = OracleSimulation(W.cavity(n=256), nthreads=8)
+    o.run(int(g["steps"]))
+    m = o.moments()
+    assert rel_err(m[:, ::4, ::4], g["sub"]).max() < 1e-11
+    assert rel_err(m[:, :2], g["lo_x"]).max() < 1e-11
+    assert rel_err(m[:, :, -2:], g["hi_y"]).max() < 1e-11
+
+
+def test_equilibrium_table_monomials():
+    from pylbm_gb300.scheme import Scheme
+    sc = Scheme(W.cavity(n=8))
+    rows, coefs, expos = equilibrium_table(sc)
+    # m3 = -2 rho + 3 qx^2 + 3 qy^2
+    sel = rows == 3
+    terms = {tuple(e): c for e, c in zip(expos[sel], coefs[sel])}
+    assert terms == {(1, 0, 0): -2.0, (0, 2, 0): 3.0, (0, 0, 2): 3.0}
+
+
+def test_planted_error_is_detected():
+    """A wrong relaxation rate in the oracle must break the parity check."""
+    g = golden("cavity_n32.npz")
+    d = W.cavity(n=32, omega=1.9)
+    o = OracleSimulation(d)
+    o.run(50)
+    assert rel_err(o.moments(), g["m50"]).max() > 1e-6
