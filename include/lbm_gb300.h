@@ -140,6 +140,20 @@ int lbm_population_sums_scratch_bytes(const lbm_lattice* lat, size_t* bytes);
 int lbm_population_sums(const void* f, const lbm_lattice* lat, double* sums, int32_t* nonfinite,
                         void* partials, size_t partials_bytes, void* stream);
 
+/* Same sums for callers that cannot call cudaMalloc (a host application
+ * whose memory manager owns every device allocation, or a time-critical loop
+ * that cannot afford cudaMalloc's implicit synchronisation): the partial sums
+ * live in a fixed 1 MiB device array inside the library (see
+ * lbm_population_sums_noalloc_max_bytes), held by every GPU that loads the
+ * library until exit.  Lattices whose partials exceed it are rejected with
+ * LBM_ERR_ARG.  The first call on a device looks up the array's address for
+ * that device; make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race.  Allocates nothing.
+ * No counterpart in the reference (pylbm has no conservation check). */
+int lbm_population_sums_noalloc(const void* f, const lbm_lattice* lat, double* sums,
+                                int32_t* nonfinite, void* stream);
+size_t lbm_population_sums_noalloc_max_bytes(void);
+
 /* ------------------------------------------------------------------ */
 /* lbm_scheme_<id>.so: per-scheme module (generated constants + the     */
 /* kernel templates of pylbm_gb300/csrc/scheme_kernels.cuh)            */

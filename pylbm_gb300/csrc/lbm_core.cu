@@ -6,6 +6,7 @@
 #include "lbm_common.cuh"
 
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 
 using namespace lbm;
@@ -463,3 +464,72 @@ int lbm_population_sums(const void* f, const lbm_lattice* lat, double* sums, int
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of lbm_population_sums.
+//
+// Some callers cannot call cudaMalloc: a host application whose own memory
+// manager owns every device allocation (the library may only use what it is
+// handed), or a time-critical loop in which the implicit device
+// synchronisation of cudaMalloc/cudaFree is not acceptable.  For them the
+// per-block partial sums live in a fixed file-scope device array instead of
+// caller-provided scratch.  The array is 1 MiB (131072 FP64 partials: any
+// lattice with nv * blocks within that, e.g. every lattice with nv <= 32) and
+// every GPU that loads this library holds it until the process exits.
+//
+// In host code the array's name is only a host-side stand-in, so its device
+// address is looked up once per device (cudaGetSymbolAddress, with that device
+// current) on the first call made on that device; that first call should come
+// before any stream capture.  All calls share the one array: calls that
+// overlap on the GPU (e.g. on two streams) race on it.  Nothing in it needs to
+// start at zero -- every partial is written before it is read -- and the
+// non-finite counter is the caller's output, cleared by the call.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(1) << 20;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocScratchBytes / sizeof(double)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_address[kMaxDevices] = {nullptr};
+
+int noalloc_scratch_address(void** out) {
+  int dev = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "lbm_population_sums_noalloc: cudaGetDevice");
+  if (rc) return rc;
+  if (dev < 0 || dev >= kMaxDevices)
+    return fail(LBM_ERR_UNSUPPORTED, "lbm_population_sums_noalloc: device %d beyond %d", dev, kMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_address[dev]) {
+    void* p = nullptr;
+    rc = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_partials),
+                    "lbm_population_sums_noalloc: cudaGetSymbolAddress");
+    if (rc) return rc;
+    g_noalloc_address[dev] = p;
+  }
+  *out = g_noalloc_address[dev];
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" size_t lbm_population_sums_noalloc_max_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" int lbm_population_sums_noalloc(const void* f, const lbm_lattice* lat, double* sums,
+                                           int32_t* nonfinite, void* stream) {
+  int rc = check_lattice(lat, "lbm_population_sums_noalloc");
+  if (rc) return rc;
+  size_t need = 0;
+  rc = lbm_population_sums_scratch_bytes(lat, &need);
+  if (rc) return rc;
+  if (need > kNoAllocScratchBytes)
+    return fail(LBM_ERR_ARG,
+                "lbm_population_sums_noalloc: this lattice needs %zu bytes of partial sums, the built-in "
+                "scratch holds %zu; use lbm_population_sums with caller-provided scratch",
+                need, kNoAllocScratchBytes);
+  void* scratch = nullptr;
+  rc = noalloc_scratch_address(&scratch);
+  if (rc) return rc;
+  return lbm_population_sums(f, lat, sums, nonfinite, scratch, kNoAllocScratchBytes, stream);
+}

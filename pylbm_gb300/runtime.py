@@ -136,6 +136,8 @@ def core():
             _sig(lib, "lbm_neumann", I32, [P, P, P, I32, LP, I32, P])
             _sig(lib, "lbm_population_sums_scratch_bytes", I32, [LP, ctypes.POINTER(SZ)])
             _sig(lib, "lbm_population_sums", I32, [P, LP, P, P, P, SZ, P])
+            _sig(lib, "lbm_population_sums_noalloc", I32, [P, LP, P, P, P])
+            _sig(lib, "lbm_population_sums_noalloc_max_bytes", SZ, [])
             _core = lib
     return _core
 
