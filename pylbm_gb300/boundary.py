@@ -113,6 +113,8 @@ class BoundaryMethod:
         else:
             func(f, m, t, *args)
         cons = m.array.reshape(sim.scheme.nv, n)[:sim.scheme.nconsm]
+        if hasattr(sim, "feq_host"):
+            return sim.feq_host(cons)
         return sim.scheme.feq_numpy(cons, sim.extra_parameters_str())
 
     def prepare_rhs(self, sim):

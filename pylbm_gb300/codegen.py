@@ -151,11 +151,23 @@ class SchemeSource:
         True: storage holds f - feq(c0) and the relaxation works on deviations.
     c0 : sequence of float
         reference values of the conserved moments (used only when shifted).
+    style : "fast" or "reference"
+        "fast": exact constants, shared pair sums, grouped coefficients.
+        "reference" (unshifted float64 only): the reference generator's
+        printed expressions (refforms.ReferenceForms), compiled without fused
+        multiply-adds, for parity with pylbm's generated code.
     """
 
-    def __init__(self, scheme, shifted, c0=None):
+    def __init__(self, scheme, shifted, c0=None, style="fast"):
         self.scheme = scheme
         self.shifted = bool(shifted)
+        if style not in ("fast", "reference"):
+            raise SchemeError(f"unknown style {style!r}")
+        if style == "reference" and self.shifted:
+            raise SchemeError("the reference style is the unshifted float64 form")
+        self.style = style
+        self.nvcc_flags = ["-fmad=false"] if style == "reference" else []
+        self._ref = None
         nv, nc = scheme.nv, scheme.nconsm
         self.c0 = [to_fraction(c) for c in (c0 if c0 is not None else [0] * nc)]
         if len(self.c0) != nc:
@@ -337,6 +349,9 @@ class SchemeSource:
         out.append("static const double lbm_host_mref[LBM_Q] = {" +
                    ", ".join(repr(float(x)) for x in self.mref) + "};")
         out.append("")
+        if self.style == "reference":
+            out += self._reference_functions()
+            return "\n".join(out) + "\n"
         # moments of a deviation vector
         out.append("template <typename R>")
         out.append("__device__ __forceinline__ void lbm_moments(const R (&g)[LBM_Q], R (&m)[LBM_Q]) {")
@@ -372,6 +387,32 @@ class SchemeSource:
         out.append("  lbm_populations<R>(m, g);")
         out.append("}")
         return "\n".join(out) + "\n"
+
+    def reference_forms(self):
+        from .refforms import ReferenceForms
+
+        if self._ref is None:
+            self._ref = ReferenceForms(self.scheme.dico, self.params)
+        return self._ref
+
+    def _reference_functions(self):
+        """Per-node functions printed as the reference generator prints them."""
+        ref = self.reference_forms()
+        ind = "  "
+
+        def fn(sig, body):
+            return ["template <typename R>", f"__device__ __forceinline__ void {sig} {{"] + \
+                   [ind + line for line in body] + [ind + "(void)prm;" if "prm" in sig else "", "}"]
+
+        out = []
+        out += fn("lbm_moments(const R (&g)[LBM_Q], R (&m)[LBM_Q])", ref.moments_full("g", "m"))
+        out += fn("lbm_populations(const R (&m)[LBM_Q], R (&g)[LBM_Q])", ref.populations_routine("m", "g"))
+        out += fn("lbm_relax_abs(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.relaxation_routine("m"))
+        out += fn("lbm_relax(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.relaxation("m"))
+        out += fn("lbm_equilibrium_abs(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.equilibrium("m"))
+        out += fn("lbm_collide(R (&g)[LBM_Q], const R* __restrict__ prm)",
+                  ["R m[LBM_Q];"] + ref.moments_pull("g", "m") + ref.relaxation("m") + ref.populations("m", "g"))
+        return out
 
     def module_source(self, storage, compute):
         """Full translation unit of the module for one storage/compute type."""

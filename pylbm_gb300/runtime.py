@@ -273,7 +273,8 @@ class SchemeModule:
         text = source_obj.module_source(storage, compute)
         deps = "".join(open(os.path.join(CSRC, f)).read() for f in ("lbm_common.cuh", "scheme_kernels.cuh"))
         deps += open(os.path.join(INCLUDE, "lbm_gb300.h")).read()
-        key = hashlib.sha256((text + deps + " ".join(ARCH_FLAGS)).encode()).hexdigest()[:20]
+        flags = list(getattr(source_obj, "nvcc_flags", []))
+        key = hashlib.sha256((text + deps + " ".join(ARCH_FLAGS + flags)).encode()).hexdigest()[:20]
         self.key = key
         self.path = os.path.join(JIT_DIR, f"lbm_scheme_{key}.so")
         with SchemeModule._lock:
@@ -285,7 +286,7 @@ class SchemeModule:
                     with open(cu + ".tmp", "w") as fh:
                         fh.write(text)
                     os.replace(cu + ".tmp", cu)
-                    _nvcc_shared([cu], self.path)
+                    _nvcc_shared([cu], self.path, extra=flags)
                 lib = ctypes.CDLL(self.path)
                 self._bind(lib)
                 SchemeModule._cache[key] = lib

@@ -102,6 +102,7 @@ class Scheme:
     def __init__(self, dico):
         if dico.get("relative_velocity") is not None:
             raise SchemeError("relative_velocity schemes are not supported by the CUDA backend")
+        self.dico = dico
         self.dim = _box_dim(dico)
         schemes = dico["schemes"]
         self.stencil = Stencil.from_dico(dico, self.dim)

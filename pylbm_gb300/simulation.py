@@ -97,10 +97,15 @@ class Simulation:
         initialise the populations now (else on the first step).
     shifted : bool or None
         store deviations from feq(c0); default: every type but float64.
+    parity : bool
+        float64 only: evaluate the per-node algebra in the reference
+        generator's printed form (refforms), compiled without FMA, so results
+        track pylbm's Cython code; False uses the faster exact-constant form.
     """
 
     def __init__(self, dico, sorder=None, dtype="float64", check_inverse=False, initialize=True,
-                 shifted=None):
+                 shifted=None, parity=True):
+        self.parity = bool(parity)
         gen = str(dico.get("generator", "cuda")).upper()
         if gen != "CUDA":
             raise ValueError(f"pylbm_gb300 implements generator='cuda', not {gen!r}")
@@ -162,6 +167,19 @@ class Simulation:
         arr = np.array([float(vals[n]) for n in names] + [0.0], dtype=np.float64)
         return arr
 
+    def feq_host(self, cons):
+        """Equilibrium populations of boundary values on the host.
+
+        In the float64 parity form they come from the reference generator's
+        printed equilibrium and m2f routines, so boundary right-hand sides
+        equal pylbm's; otherwise from the exact-constant matrices.
+        """
+        params = self.extra_parameters_str()
+        if self.module is not None and self.module.src.style == "reference":
+            prm = [float(params[str(s)]) for s in self.scheme.free_symbols]
+            return self.module.src.reference_forms().feq_host(cons, prm)
+        return self.scheme.feq_numpy(cons, params)
+
     def _mbuf(self):
         if self._M is None:
             self._M = runtime.DeviceBuffer(self._mlat.elements * 8)
@@ -213,7 +231,8 @@ class Simulation:
             arr = np.einsum("ij,j...->i...", sc.M, arr)
         inner = tuple(slice(int(h), -int(h)) for h in self.domain.halo)
         c0 = [_round_reference(arr[c][inner]) for c in range(sc.nconsm)] if self.shifted else None
-        src = SchemeSource(sc, self.shifted, c0)
+        style = "reference" if (self.storage == "float64" and not self.shifted and self.parity) else "fast"
+        src = SchemeSource(sc, self.shifted, c0, style=style)
         self.module = runtime.SchemeModule(src, self.storage, self.compute)
         for k in range(nv):
             self._lat.shift[k] = float(self.module.shift[k])

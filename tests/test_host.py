@@ -164,3 +164,47 @@ def test_c_abi_rejects_bad_arguments_without_gpu():
     good = runtime.lattice(2, 9, "float64", [8, 8], [1, 1])
     good.n[0] = 0
     assert lib.lbm_update_halo(None, ctypes.byref(good), None) == 1
+
+
+def test_reference_forms_reproduce_generated_boundary_rhs():
+    """Boundary right-hand sides from the printed reference forms equal pylbm's bit for bit."""
+    from pylbm_gb300.refforms import ReferenceForms
+    for fixture, d in (("cavity_n32.npz", W.cavity(n=32)),
+                       ("cylinder_small.npz", W.cylinder(nx=96, ny=32, radius=5, center=(24, 17), re=40.0))):
+        g = golden(fixture)
+        sim = _HostSim(d)
+        rf = ReferenceForms(d)
+        sim.feq_host = lambda cons, rf=rf: rf.feq_host(cons)
+        bc = Boundary(sim.domain, d)
+        for i, meth in enumerate(bc.methods):
+            meth.set_iload()
+            meth.prepare_rhs(sim)
+            meth.fix_iload()
+            meth.set_rhs()
+            assert np.array_equal(meth.rhs, g[f"bc{i}_rhs"])
+
+
+def test_reference_forms_print_like_the_generator():
+    """Spot checks of the printed constants and term order of the reference generator."""
+    from pylbm_gb300.refforms import ReferenceForms
+    rf = ReferenceForms(W.cavity(n=32))
+    relax = rf.relaxation()
+    assert relax[0] == ("m[3] = -4.5*(0.666666666666667*m[0] - 1.0*(m[1]*m[1]) - 1.0*(m[2]*m[2]) "
+                        "+ 0.111111111111111*m[3]);")
+    assert rf.populations()[0] == ("g[0] = (0.1111111111111111)*m[0] - 0.111111111111111*m[3] "
+                                   "+ 0.111111111111111*m[4];")
+    assert rf.moments_pull()[0].startswith("m[0] = g[7] + g[6] + g[3] + g[8]")
+    # the standalone m2f routine orders indexed moments by their printed index
+    r3 = ReferenceForms(W.tgv3d(n=8))
+    line = r3.populations_routine()[1]
+    assert line.index("m[10]") < line.index("m[3]")
+
+
+def test_fast_and_reference_styles_share_constants():
+    sc = Scheme(W.cavity(n=8))
+    fast = SchemeSource(sc, shifted=False)
+    ref = SchemeSource(sc, shifted=False, style="reference")
+    assert ref.nvcc_flags == ["-fmad=false"] and fast.nvcc_flags == []
+    assert "0.666666666666667" in ref.header()
+    with pytest.raises(SchemeError):
+        SchemeSource(sc, shifted=True, c0=[1, 0, 0], style="reference")
