@@ -137,17 +137,59 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def time_steps(sim, steps):
+    """Device time (ms) of ``steps`` steps replayed from the captured graph."""
+    from pylbm_gb300 import runtime
+
+    sim.run(2)  # capture outside the timed region
+    sim.synchronize()
+    e0, e1 = runtime.Event(), runtime.Event()
+    e0.record(sim._stream)
+    sim.run(steps)
+    e1.record(sim._stream)
+    return e0.elapsed_ms(e1)
+
+
+def variants(args):
+    """The other configurations: MLUPS and HBM fraction of each (bounded runs)."""
+    from pylbm_gb300 import Simulation
+    from pylbm_gb300 import workloads as W
+
+    peak, _ = measured_peaks()
+    out = {}
+    cases = [
+        ("tgv3d_256_f64", lambda: Simulation(W.tgv3d(n=256), dtype="float64", parity=False), 256 ** 3, 19, 8, 40),
+        ("tgv3d_256_f16", lambda: Simulation(W.tgv3d(n=256), dtype="float16"), 256 ** 3, 19, 2, 100),
+        ("tgv3d_256_bf16", lambda: Simulation(W.tgv3d(n=256), dtype="bfloat16"), 256 ** 3, 19, 2, 100),
+        ("cavity_256_f64_parity", lambda: Simulation(W.cavity(n=256)), 256 ** 2, 9, 8, 1000),
+        ("cylinder_2048x512_f32", lambda: Simulation(W.cylinder(), dtype="float32"), 2048 * 512, 9, 4, 1000),
+    ]
+    for name, make, nodes, q, es, steps in cases:
+        sim = make()
+        for _ in range(3):
+            sim.one_time_step()
+        ms = time_steps(sim, steps)
+        mlups = nodes * steps / (ms / 1e3) / 1e6
+        gbs = 2 * q * es * nodes * steps / (ms / 1e3) / 1e9
+        out[name] = {"MLUPS": mlups, "ms_per_step": ms / steps, "GB/s": gbs, "hbm_frac": gbs / peak,
+                     "steps": steps}
+        sim.free()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256, help="grid size per axis")
     ap.add_argument("--dtype", default="float32", choices=list(BYTES_PER_VALUE))
-    ap.add_argument("--cpu-grid", type=int, default=128)
+    ap.add_argument("--cpu-grid", type=int, default=256)
+    ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -176,6 +218,7 @@ def main():
     assert sim.periodic
     for _ in range(args.warmup):
         sim.one_time_step()
+    sim.run(2)  # graph capture outside the timed region
     sim.synchronize()
     if dist:
         dist.barrier()
@@ -184,38 +227,32 @@ def main():
     time.sleep(0.3)
     e0, e1 = runtime.Event(), runtime.Event()
     e0.record(sim._stream)
-    for _ in range(args.steps):
-        sim.one_time_step()
+    sim.run(args.steps)
     e1.record(sim._stream)
     ms = e0.elapsed_ms(e1)
     clocks = sampler.stop()
-    sim.synchronize()
-    times = [ms]
     if dist:
         import torch
         t = torch.tensor([ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        times = [float(t.item())]
-    ms_total = times[0]
-    ms_step = ms_total / args.steps
-    value = nodes * args.steps * world / (ms_total / 1e3) / 1e6
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = nodes * args.steps * world / (ms / 1e3) / 1e6
     bpl = 2 * sim.scheme.nv * BYTES_PER_VALUE[args.dtype]
     achieved = bpl * nodes / (ms_step / 1e3) / 1e9
     peak, peak_src = measured_peaks()
-    traffic = profiled_traffic(f"ncu_step_tgv3d_{DTYPE_TAG[args.dtype]}.txt") if n == 256 else None
+    traffic = profiled_traffic(f"ncu_step_tgv3d_{DTYPE_TAG[args.dtype]}.md") if n == 256 else None
 
-    e2e = None
-    if not args.no_e2e:
-        e2e = end_to_end(sim, args, nodes)
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_reference(args, steps=3, sample_grid=args.cpu_grid)
-
-    # check the result is sane (mass conserved, finite)
     sums, bad = sim.population_sums()
     if bad:
         raise FloatingPointError("non-finite populations after the timed steps")
+
+    e2e = None if args.no_e2e else end_to_end(sim, args, nodes)
+    sim.free()
+    var = None if (args.no_variants or rank != 0) else variants(args)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_reference(args, steps=args.cpu_steps, sample_grid=args.cpu_grid)
 
     if rank == 0:
         line = {
@@ -225,7 +262,8 @@ def main():
             "config": {"workload": f"D3Q19 MRT periodic Taylor-Green vortex {n}^3, {args.dtype} shifted storage, "
                                    f"{'f64' if args.dtype == 'float64' else 'f32'} arithmetic",
                        "grid": [n, n, n], "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (%.2f GB per population buffer)" % (sim._F.nbytes / 1e9)},
+                       "l2": "inputs larger than L2 (%.2f GB per population buffer), no flush needed"
+                             % (2 * sim.scheme.nv * BYTES_PER_VALUE[args.dtype] * (n + 2) ** 3 / 2 / 1e9)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_src, "bytes_per_lup": bpl,
@@ -237,6 +275,8 @@ def main():
             line["e2e"] = e2e
         if cpu:
             line["cpu_baseline"] = cpu
+        if var:
+            line["variants"] = var
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -245,31 +285,33 @@ def main():
 def end_to_end(sim, args, nodes):
     """Same metric through the public API with host buffers.
 
-    Timed: upload of the initial populations from pinned host memory, K
-    calls of Simulation.one_time_step(), download of the conserved moments
-    (rho, qx, qy, qz) of the final state -- copies inside the timed region.
+    Timed: upload of the initial populations from pinned host memory,
+    Simulation.run(K) (graph replay of the step), f2m and download of the
+    conserved moments (rho, qx, qy, qz) of the final state.
     """
     from pylbm_gb300 import runtime
 
-    es = BYTES_PER_VALUE[args.dtype]
+    core = runtime.core()
     nbytes = sim._F.nbytes
     pinned = runtime.PinnedBuffer(nbytes)
-    runtime.check(runtime.core().lbm_memcpy(ctypes.c_void_p(pinned.ptr), sim._F.handle, nbytes, runtime.D2H, None))
-    out = runtime.PinnedBuffer(8 * sim._mlat.vstride * sim.scheme.nconsm)
+    runtime.check(core.lbm_memcpy(ctypes.c_void_p(pinned.ptr), sim._F.handle, nbytes, runtime.D2H, sim._stream))
+    d2h = 8 * sim._mlat.vstride * sim.scheme.nconsm
+    out = runtime.PinnedBuffer(d2h)
     sim.synchronize()
     t0 = time.perf_counter()
-    runtime.check(runtime.core().lbm_memcpy(sim._F.handle, ctypes.c_void_p(pinned.ptr), nbytes, runtime.H2D, None))
-    for _ in range(args.steps):
-        sim.one_time_step()
+    runtime.check(core.lbm_memcpy(sim._F.handle, ctypes.c_void_p(pinned.ptr), nbytes, runtime.H2D, sim._stream))
+    sim.run(args.steps)
     sim.module.call(sim.module.lib.lbm_f2m(sim._F.handle, ctypes.byref(sim._lat), sim._mbuf().handle,
-                                           ctypes.byref(sim._mlat), None))
-    d2h = 8 * sim._mlat.vstride * sim.scheme.nconsm
-    runtime.check(runtime.core().lbm_memcpy(ctypes.c_void_p(out.ptr), sim._mbuf().handle, d2h, runtime.D2H, None))
+                                           ctypes.byref(sim._mlat), sim._stream))
+    runtime.check(core.lbm_memcpy(ctypes.c_void_p(out.ptr), sim._mbuf().handle, d2h, runtime.D2H, sim._stream))
     sim.synchronize()
     dt = time.perf_counter() - t0
+    pinned.free()
+    out.free()
     return {"value": nodes * args.steps / dt / 1e6, "unit": "MLUPS",
             "h2d_bytes_per_step": nbytes / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-            "note": f"pinned H2D of the initial state, {args.steps} API steps, D2H of the conserved moments"}
+            "note": f"pinned H2D of the initial state, run({args.steps}) through the public API, "
+                    "D2H of the conserved moments"}
 
 
 if __name__ == "__main__":

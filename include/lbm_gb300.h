@@ -90,7 +90,7 @@ int lbm_alloc(void** ptr, size_t bytes);
 int lbm_free(void* ptr);
 int lbm_memcpy(void* dst, const void* src, size_t bytes, int32_t kind, void* stream);
 int lbm_memset(void* ptr, int32_t value, size_t bytes, void* stream);
-int lbm_stream_create(void** stream);
+int lbm_stream_create(void** stream); /* blocking: ordered with the legacy default stream */
 int lbm_stream_destroy(void* stream);
 int lbm_stream_synchronize(void* stream);
 
@@ -103,6 +103,16 @@ int lbm_event_create(void** event);
 int lbm_event_destroy(void* event);
 int lbm_event_record(void* event, void* stream);
 int lbm_event_elapsed_ms(void* start, void* end, float* ms); /* synchronizes on `end` */
+
+/* CUDA graphs: capture the work enqueued on `stream` (not the legacy default
+ * stream) between lbm_graph_begin and lbm_graph_end into an executable
+ * graph, then replay it with lbm_graph_launch.  Used to replay a fixed
+ * sequence of steps (ghost refresh, boundary kernels, step kernel) with one
+ * launch. */
+int lbm_graph_begin(void* stream);
+int lbm_graph_end(void* stream, void** graph_exec);
+int lbm_graph_launch(void* graph_exec, void* stream);
+int lbm_graph_destroy(void* graph_exec);
 
 /* Periodic ghost refresh of every axis: ghost layer i of an axis receives
  * interior layer i +/- n (pylbm/storage.py:307-367 Array.update, a periodic

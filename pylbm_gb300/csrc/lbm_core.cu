@@ -329,7 +329,9 @@ int lbm_memset(void* ptr, int32_t value, size_t bytes, void* stream) {
 int lbm_stream_create(void** stream) {
   if (!stream) return fail(LBM_ERR_ARG, "lbm_stream_create: NULL");
   cudaStream_t s;
-  int rc = cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+  // a blocking stream: work on it is ordered with the legacy default stream,
+  // so callers that mix both (e.g. NULL-stream copies) stay race-free
+  int rc = cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamDefault), "cudaStreamCreate");
   *stream = rc ? nullptr : (void*)s;
   return rc;
 }
@@ -377,6 +379,36 @@ int lbm_event_elapsed_ms(void* start, void* end, float* ms) {
   int rc = cuda_check(cudaEventSynchronize((cudaEvent_t)end), "cudaEventSynchronize");
   if (rc) return rc;
   return cuda_check(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)end), "cudaEventElapsedTime");
+}
+
+int lbm_graph_begin(void* stream) {
+  if (!stream) return fail(LBM_ERR_ARG, "lbm_graph_begin: capture needs a created stream, not NULL");
+  return cuda_check(cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal),
+                    "cudaStreamBeginCapture");
+}
+
+int lbm_graph_end(void* stream, void** graph_exec) {
+  if (!stream || !graph_exec) return fail(LBM_ERR_ARG, "lbm_graph_end: NULL argument");
+  *graph_exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int rc = cuda_check(cudaStreamEndCapture((cudaStream_t)stream, &graph), "cudaStreamEndCapture");
+  if (rc) return rc;
+  cudaGraphExec_t exec = nullptr;
+  rc = cuda_check(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+  cudaGraphDestroy(graph);
+  if (rc) return rc;
+  *graph_exec = (void*)exec;
+  return LBM_OK;
+}
+
+int lbm_graph_launch(void* graph_exec, void* stream) {
+  if (!graph_exec) return fail(LBM_ERR_ARG, "lbm_graph_launch: NULL graph");
+  return cuda_check(cudaGraphLaunch((cudaGraphExec_t)graph_exec, (cudaStream_t)stream), "cudaGraphLaunch");
+}
+
+int lbm_graph_destroy(void* graph_exec) {
+  if (!graph_exec) return LBM_OK;
+  return cuda_check(cudaGraphExecDestroy((cudaGraphExec_t)graph_exec), "cudaGraphExecDestroy");
 }
 
 int lbm_update_halo(void* f, const lbm_lattice* lat, void* stream) {

@@ -130,6 +130,10 @@ def core():
             _sig(lib, "lbm_event_destroy", I32, [P])
             _sig(lib, "lbm_event_record", I32, [P, P])
             _sig(lib, "lbm_event_elapsed_ms", I32, [P, P, ctypes.POINTER(ctypes.c_float)])
+            _sig(lib, "lbm_graph_begin", I32, [P])
+            _sig(lib, "lbm_graph_end", I32, [P, ctypes.POINTER(P)])
+            _sig(lib, "lbm_graph_launch", I32, [P, P])
+            _sig(lib, "lbm_graph_destroy", I32, [P])
             _sig(lib, "lbm_update_halo", I32, [P, LP, P])
             _sig(lib, "lbm_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_anti_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
@@ -191,8 +195,7 @@ class DeviceBuffer:
             raise ValueError("upload larger than the buffer")
         check(core().lbm_memcpy(ctypes.c_void_p(self.ptr + offset), a.ctypes.data_as(ctypes.c_void_p), a.nbytes,
                                 H2D, stream))
-        if stream is None:
-            check(core().lbm_stream_synchronize(None))
+        check(core().lbm_stream_synchronize(stream))
         return a
 
     def download(self, out, stream=None, offset=0):

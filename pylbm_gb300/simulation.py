@@ -13,6 +13,9 @@ on the device in the padded structure-of-arrays layout of the C ABI; a step is
 
 and a domain that is periodic along every axis skips the first two and uses
 ``lbm_one_time_step_periodic``, which wraps the pull inside the interior.
+``run(n)`` replays a captured CUDA graph of two steps (the buffers are back in
+place after two swaps), so a step costs one graph launch instead of one
+Python call and 2 + nmethods kernel launches.
 
 ``dtype`` selects the storage type: "float64" (FP64 storage and arithmetic,
 the parity path) or "float32"/"float16"/"bfloat16" (values stored as
@@ -59,8 +62,8 @@ def _round_reference(values):
     return float(f"{mean:.4g}")
 
 
-def _to_storage(host, dtype):
-    """float64 numpy -> raw storage array of ``dtype``."""
+def to_storage(host, dtype):
+    """float64 numpy -> raw storage array of ``dtype`` (bfloat16 as uint16 bits)."""
     if dtype == "float64":
         return np.ascontiguousarray(host, dtype=np.float64)
     if dtype == "float32":
@@ -73,13 +76,13 @@ def _to_storage(host, dtype):
     return ((b + rounding) >> 16).astype(np.uint16)
 
 
-def _from_storage(raw, dtype):
+def from_storage(raw, dtype):
     if dtype == "bfloat16":
         return (raw.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
     return raw.astype(np.float64)
 
 
-_RAW = {"float64": np.float64, "float32": np.float32, "float16": np.float16, "bfloat16": np.uint16}
+RAW_DTYPE = {"float64": np.float64, "float32": np.float32, "float16": np.float16, "bfloat16": np.uint16}
 
 
 class Simulation:
@@ -105,12 +108,12 @@ class Simulation:
 
     def __init__(self, dico, sorder=None, dtype="float64", check_inverse=False, initialize=True,
                  shifted=None, parity=True):
-        self.parity = bool(parity)
         gen = str(dico.get("generator", "cuda")).upper()
         if gen != "CUDA":
             raise ValueError(f"pylbm_gb300 implements generator='cuda', not {gen!r}")
         if dtype not in _STORAGES:
             raise ValueError(f"dtype must be one of {_STORAGES}")
+        self.parity = bool(parity)
         self.dico = dico
         self.scheme = Scheme(dico)
         self.domain = Domain(dico, self.scheme.stencil)
@@ -138,14 +141,18 @@ class Simulation:
         self._lat = runtime.lattice(self.dim, self.scheme.nv, dtype, shape_in, halo)
         self._mlat = runtime.lattice(self.dim, self.scheme.nv, "float64", shape_in, halo)
         es = runtime.DTYPE_SIZE[dtype]
+        s = ctypes.c_void_p()
+        runtime.check(self._core.lbm_stream_create(ctypes.byref(s)))
+        self._stream = s
         self._F = runtime.DeviceBuffer(self._lat.elements * es)
         self._Fnew = runtime.DeviceBuffer(self._lat.elements * es)
         self._M = None
-        self._stream = None
         self.module = None
         self._m_cache = {}
         self._update_m = True
         self._bc_dev = []
+        self._graph = None
+        self._graph_key = None
         self._need_init = True
         if initialize:
             self._initialize()
@@ -164,8 +171,7 @@ class Simulation:
         missing = [n for n in names if n not in vals]
         if missing:
             raise ValueError(f"extra_parameters must give values for {missing}")
-        arr = np.array([float(vals[n]) for n in names] + [0.0], dtype=np.float64)
-        return arr
+        return np.array([float(vals[n]) for n in names] + [0.0], dtype=np.float64)
 
     def feq_host(self, cons):
         """Equilibrium populations of boundary values on the host.
@@ -185,21 +191,11 @@ class Simulation:
             self._M = runtime.DeviceBuffer(self._mlat.elements * 8)
         return self._M
 
-    def _halo_view(self, flat, lat, nv=None):
-        """View of a downloaded padded buffer as (nv, *shape_halo)."""
-        nv = lat.nv if nv is None else nv
-        shape = [nv] + self.domain.shape_halo
-        strides_el = [lat.vstride] + [lat.stride[d] for d in range(self.dim)]
-        es = flat.itemsize
-        return np.lib.stride_tricks.as_strided(flat[lat.origin:], shape=shape,
-                                               strides=[s * es for s in strides_el])
-
-    def _padded(self, arr, lat, dtype):
-        """Pack (nv, *shape_halo) values into a padded flat buffer of ``lat``."""
-        flat = np.zeros(lat.elements, dtype=dtype)
-        view = self._halo_view(flat, lat, arr.shape[0])
-        view[...] = arr
-        return flat
+    def _plane_view(self, plane, lat):
+        """(shape_halo) view of one population plane of a padded buffer."""
+        es = plane.itemsize
+        return np.lib.stride_tricks.as_strided(plane[lat.origin:], shape=self.domain.shape_halo,
+                                               strides=[lat.stride[d] * es for d in range(self.dim)])
 
     def _initialize(self):
         sc = self.scheme
@@ -240,16 +236,17 @@ class Simulation:
         plane = np.zeros(self._mlat.vstride, dtype=np.float64)
         for c in range(nplanes):
             self._plane_view(plane, self._mlat)[...] = arr[c]
-            mbuf.upload(plane, offset=c * self._mlat.vstride * 8)
+            mbuf.upload(plane, offset=c * self._mlat.vstride * 8, stream=self._stream)
         del arr
         prm = self._prm()
         pp = prm.ctypes.data_as(ctypes.c_void_p)
         if self.init_type == "moments":
-            self.module.call(self.module.lib.lbm_equilibrium(mbuf.handle, ctypes.byref(self._mlat), pp, None))
+            self.module.call(self.module.lib.lbm_equilibrium(mbuf.handle, ctypes.byref(self._mlat), pp, self._stream))
         self.module.call(self.module.lib.lbm_m2f(mbuf.handle, ctypes.byref(self._mlat), self._F.handle,
-                                                 ctypes.byref(self._lat), None))
-        runtime.check(self._core.lbm_memcpy(self._Fnew.handle, self._F.handle, self._F.nbytes, runtime.D2D, None))
-        runtime.check(self._core.lbm_stream_synchronize(None))
+                                                 ctypes.byref(self._lat), self._stream))
+        runtime.check(self._core.lbm_memcpy(self._Fnew.handle, self._F.handle, self._F.nbytes, runtime.D2D,
+                                            self._stream))
+        self.synchronize()
         for meth in self.bc.methods:
             meth.prepare_rhs(self)
             meth.fix_iload()
@@ -257,17 +254,18 @@ class Simulation:
         self._upload_bc()
         self._update_m = True
         self._m_cache = {}
+        self._drop_graph()
         self._need_init = False
 
     def _upload_bc(self):
         self._bc_dev = []
         for meth in self.bc.methods:
             il = runtime.DeviceBuffer(max(meth.iload[0].nbytes, 4))
-            il.upload(meth.iload[0])
+            il.upload(meth.iload[0], stream=self._stream)
             st = runtime.DeviceBuffer(max(meth.istore.nbytes, 4))
-            st.upload(meth.istore)
+            st.upload(meth.istore, stream=self._stream)
             rhs = runtime.DeviceBuffer(max(meth.rhs.nbytes, 8))
-            rhs.upload(meth.rhs)
+            rhs.upload(meth.rhs, stream=self._stream)
             ordered = 0 if self._links_independent(meth) else 1
             self._bc_dev.append((meth, il, st, rhs, ordered))
 
@@ -278,26 +276,37 @@ class Simulation:
         return not any(tuple(r) in st for r in meth.iload[0].tolist())
 
     # ------------------------------------------------------------------ step
+    def _enqueue_boundary(self, F):
+        lat = ctypes.byref(self._lat)
+        runtime.check(self._core.lbm_update_halo(F.handle, lat, self._stream))
+        for meth, il, st, rhs, ordered in self._bc_dev:
+            if meth.kind == "bounce_back":
+                rc = self._core.lbm_bounce_back(F.handle, il.handle, st.handle, meth.ncond, rhs.handle, lat,
+                                                ordered, self._stream)
+            elif meth.kind == "anti_bounce_back":
+                rc = self._core.lbm_anti_bounce_back(F.handle, il.handle, st.handle, meth.ncond, rhs.handle,
+                                                     lat, ordered, self._stream)
+            else:
+                rc = self._core.lbm_neumann(F.handle, il.handle, st.handle, meth.ncond, lat, ordered,
+                                            self._stream)
+            runtime.check(rc)
+
+    def _enqueue_step(self, F, Fnew, prm):
+        if not self.periodic:
+            self._enqueue_boundary(F)
+        pp = prm.ctypes.data_as(ctypes.c_void_p)
+        fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
+        self.module.call(fn(F.handle, Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
+
     def boundary_condition(self):
         """Ghost refresh then every boundary method (pylbm/simulation.py:374-390)."""
         if self.periodic:
             return
-        lat = ctypes.byref(self._lat)
-        runtime.check(self._core.lbm_update_halo(self._F.handle, lat, self._stream))
         for meth, il, st, rhs, ordered in self._bc_dev:
             if meth.update_feq(self):
                 meth.set_rhs()
-                rhs.upload(meth.rhs)
-            if meth.kind == "bounce_back":
-                rc = self._core.lbm_bounce_back(self._F.handle, il.handle, st.handle, meth.ncond, rhs.handle, lat,
-                                                ordered, self._stream)
-            elif meth.kind == "anti_bounce_back":
-                rc = self._core.lbm_anti_bounce_back(self._F.handle, il.handle, st.handle, meth.ncond, rhs.handle,
-                                                     lat, ordered, self._stream)
-            else:
-                rc = self._core.lbm_neumann(self._F.handle, il.handle, st.handle, meth.ncond, lat, ordered,
-                                            self._stream)
-            runtime.check(rc)
+                rhs.upload(meth.rhs, stream=self._stream)
+        self._enqueue_boundary(self._F)
 
     def one_time_step(self):
         """One time step (pylbm/simulation.py:393-420)."""
@@ -314,8 +323,47 @@ class Simulation:
         self.t += self.dt
         self.nt += 1
 
-    def run(self, nsteps):
-        for _ in range(int(nsteps)):
+    def _drop_graph(self):
+        if self._graph is not None:
+            self._core.lbm_graph_destroy(self._graph)
+        self._graph = None
+        self._graph_key = None
+
+    def _capture(self, prm):
+        """Capture two steps (F -> Fnew -> F) into one executable graph."""
+        self._drop_graph()
+        runtime.check(self._core.lbm_graph_begin(self._stream))
+        try:
+            self._enqueue_step(self._F, self._Fnew, prm)
+            self._enqueue_step(self._Fnew, self._F, prm)
+        finally:
+            g = ctypes.c_void_p()
+            rc = self._core.lbm_graph_end(self._stream, ctypes.byref(g))
+        runtime.check(rc)
+        self._graph = g
+        self._graph_key = (self._F.ptr, self._Fnew.ptr, tuple(prm))
+
+    def run(self, nsteps, graph=True):
+        """Advance ``nsteps`` time steps (same result as calling one_time_step)."""
+        if self._need_init:
+            self._initialize()
+        nsteps = int(nsteps)
+        timed = any(meth._timed for meth in self.bc.methods)
+        if not graph or timed or nsteps < 2:
+            for _ in range(nsteps):
+                self.one_time_step()
+            return
+        prm = self._prm()
+        if self._graph_key != (self._F.ptr, self._Fnew.ptr, tuple(prm)):
+            self._capture(prm)
+        for _ in range(nsteps // 2):
+            runtime.check(self._core.lbm_graph_launch(self._graph, self._stream))
+            self.t += self.dt
+            self.t += self.dt
+            self.nt += 2
+        self._update_m = True
+        self._m_cache = {}
+        if nsteps % 2:
             self.one_time_step()
 
     def synchronize(self):
@@ -328,20 +376,13 @@ class Simulation:
             self._m_cache = {}
             mbuf = self._mbuf()
             self.module.call(self.module.lib.lbm_f2m(self._F.handle, ctypes.byref(self._lat), mbuf.handle,
-                                                     ctypes.byref(self._mlat), None))
+                                                     ctypes.byref(self._mlat), self._stream))
             self._update_m = False
         if idx not in self._m_cache:
             plane = np.empty(self._mlat.vstride, dtype=np.float64)
-            self._mbuf().download(plane, offset=idx * self._mlat.vstride * 8)
-            view = self._plane_view(plane, self._mlat)
-            self._m_cache[idx] = np.array(view)
+            self._mbuf().download(plane, offset=idx * self._mlat.vstride * 8, stream=self._stream)
+            self._m_cache[idx] = np.array(self._plane_view(plane, self._mlat))
         return self._m_cache[idx]
-
-    def _plane_view(self, plane, lat):
-        shape = self.domain.shape_halo
-        es = plane.itemsize
-        return np.lib.stride_tricks.as_strided(plane[lat.origin:], shape=shape,
-                                               strides=[lat.stride[d] * es for d in range(self.dim)])
 
     def _inner(self):
         return tuple(slice(int(h), -int(h)) for h in self.domain.halo)
@@ -358,9 +399,9 @@ class Simulation:
     def _population_halo(self, k):
         k = int(k)
         es = runtime.DTYPE_SIZE[self.storage]
-        raw = np.empty(self._lat.vstride, dtype=_RAW[self.storage])
-        self._F.download(raw, offset=k * self._lat.vstride * es)
-        vals = _from_storage(raw, self.storage)
+        raw = np.empty(self._lat.vstride, dtype=RAW_DTYPE[self.storage])
+        self._F.download(raw, offset=k * self._lat.vstride * es, stream=self._stream)
+        vals = from_storage(raw, self.storage)
         return np.array(self._plane_view(vals, self._lat)) + float(self._lat.shift[k])
 
     def _set_population_halo(self, k, value):
@@ -370,7 +411,7 @@ class Simulation:
         es = runtime.DTYPE_SIZE[self.storage]
         plane = np.zeros(self._lat.vstride, dtype=np.float64)
         self._plane_view(plane, self._lat)[...] = cur - float(self._lat.shift[k])
-        self._F.upload(_to_storage(plane, self.storage), offset=k * self._lat.vstride * es)
+        self._F.upload(to_storage(plane, self.storage), offset=k * self._lat.vstride * es, stream=self._stream)
         self._update_m = True
         self._m_cache = {}
 
@@ -407,6 +448,7 @@ class Simulation:
         return self.scheme.M[:self.scheme.nconsm] @ sums
 
     def free(self):
+        self._drop_graph()
         for b in (self._F, self._Fnew, self._M):
             if b is not None:
                 b.free()
@@ -415,3 +457,12 @@ class Simulation:
             st.free()
             rhs.free()
         self._bc_dev = []
+        if self._stream:
+            self._core.lbm_stream_destroy(self._stream)
+            self._stream = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

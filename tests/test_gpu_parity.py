@@ -23,19 +23,28 @@ def _gpu_moments(sim):
 
 
 def test_cavity_fp64_matches_reference_and_oracle():
+    """Parity form: bit-identical to pylbm's Cython output (bound asked for: 1e-12)."""
     g = golden("cavity_n32.npz")
     sim = Simulation(W.cavity(n=32))
-    assert rel_err(_gpu_moments(sim), g["m0"]).max() < 1e-14
+    assert np.array_equal(_gpu_moments(sim), g["m0"])
     o = OracleSimulation(W.cavity(n=32))
     o.initialize()
     sim.run(50)
     o.run(50)
-    assert rel_err(_gpu_moments(sim), g["m50"]).max() < 1e-12
+    assert np.array_equal(_gpu_moments(sim), g["m50"])
     assert rel_err(_gpu_moments(sim), o.moments()).max() < 1e-12
     sim.run(250)
     o.run(250)
-    assert rel_err(_gpu_moments(sim), g["m300"]).max() < 2e-12
+    assert np.array_equal(_gpu_moments(sim), g["m300"])
     assert rel_err(_gpu_moments(sim), o.moments()).max() < 2e-12
+
+
+def test_cavity_fast_form_within_tolerance():
+    """The exact-constant FP64 form (parity=False) stays within 2e-12 after 300 steps."""
+    g = golden("cavity_n32.npz")
+    sim = Simulation(W.cavity(n=32), parity=False)
+    sim.run(300)
+    assert rel_err(_gpu_moments(sim), g["m300"]).max() < 2e-12
 
 
 def test_cylinder_fp64_boundaries_match_reference():
@@ -44,23 +53,25 @@ def test_cylinder_fp64_boundaries_match_reference():
     g = golden("cylinder_small.npz")
     sim = Simulation(d)
     sim.run(100)
-    assert rel_err(_gpu_moments(sim), g["m100"]).max() < 5e-12
+    assert np.array_equal(_gpu_moments(sim), g["m100"])
 
 
 def test_tgv3d_fp64_matches_reference():
     g = golden("tgv3d_n16.npz")
     sim = Simulation(W.tgv3d(n=16))
     assert sim.periodic
-    assert rel_err(_gpu_moments(sim), g["m0"]).max() < 1e-12
+    assert rel_err(_gpu_moments(sim), g["m0"]).max() < 1e-14
     sim.run(20)
-    assert rel_err(_gpu_moments(sim), g["m20"]).max() < 5e-12
+    assert rel_err(_gpu_moments(sim), g["m20"]).max() < 1e-14
 
 
 def test_shear_layer_fp64_matches_reference():
     g = golden("shear_n64.npz")
     sim = Simulation(W.shear_layer(n=64))
     sim.run(200)
-    assert rel_err(_gpu_moments(sim), g["m200"]).max() < 5e-12
+    # bit-identical on the GB300 host; the bound leaves room for the last bit
+    # of the host libm's tanh/sin in the initial data
+    assert rel_err(_gpu_moments(sim), g["m200"]).max() < 1e-14
 
 
 def test_periodic_kernel_equals_ghost_kernel():
@@ -176,3 +187,18 @@ def test_cavity_full_size_fp64_against_reference():
     e = max(rel_err(m[:, ::4, ::4], g["sub"]).max(), rel_err(m[:, :2], g["lo_x"]).max(),
             rel_err(m[:, :, -2:], g["hi_y"]).max())
     assert e <= 1e-12, e
+    assert np.array_equal(m[:, ::4, ::4], g["sub"])
+
+
+@pytest.mark.parametrize("make", [lambda: Simulation(W.cavity(n=48)),
+                                  lambda: Simulation(W.shear_layer(n=48), dtype="float32"),
+                                  lambda: Simulation(W.cylinder(nx=64, ny=24, radius=4, center=(16, 12), re=30.0),
+                                                     dtype="float16")])
+def test_graph_replay_equals_step_loop(make):
+    """run(n) replays a captured graph of two steps; it must equal n one_time_step calls bit for bit."""
+    a, b = make(), make()
+    a.run(37)
+    for _ in range(37):
+        b.one_time_step()
+    assert a.nt == b.nt == 37 and a.t == b.t
+    assert np.array_equal(_gpu_moments(a), _gpu_moments(b))

@@ -39,11 +39,13 @@ def test_noalloc_sums_match_allocating_sums_twice():
     results = []
     for call in range(2):
         sim.run(5 + 10 * call)  # different contents for the second call
+        sim.synchronize()
         runtime.check(core.lbm_population_sums(sim._F.handle, lat, out_ref.handle,
                                                ctypes.c_void_p(out_ref.ptr + 8 * nv), scratch.handle,
-                                               size.value, None))
+                                               size.value, sim._stream))
         runtime.check(core.lbm_population_sums_noalloc(sim._F.handle, lat, out_na.handle,
-                                                       ctypes.c_void_p(out_na.ptr + 8 * nv), None))
+                                                       ctypes.c_void_p(out_na.ptr + 8 * nv), sim._stream))
+        sim.synchronize()
         ref, ref_flag = _read(out_ref, nv)
         got, got_flag = _read(out_na, nv)
         assert got_flag == ref_flag == 0
