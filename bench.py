@@ -9,8 +9,14 @@ every step streams from HBM.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
---impl reference times the CPU restatement of the reference algorithm (the
-C oracle, all host cores, OpenMP) on a bounded sample of the same workload.
+--impl reference times the reference's own CPU implementation of the step:
+pylbm's generated Cython one_time_step for this scheme (oracle/_ref, compiled
+for the host by __graft_entry__.build()), one x-slab of the 256^3 grid per
+host core as pylbm's MPI decomposition would split it, on a bounded number of
+steps; without oracle/_ref it times the C oracle (OpenMP) instead.  The same
+measurement is the ``cpu_baseline`` of the default line.  The default line
+also carries ``variants``: the FP64/FP16/BF16 storage forms of the same
+workload, the FP64 parity-form 256^2 cavity and the FP32 2048x512 disc flow.
 With N > 1 (torchrun) every rank runs an independent replica (the path has
 no cross-GPU exchange); value = total nodes updated by all ranks / max time.
 """
@@ -106,29 +112,21 @@ class ClockSampler:
 
 
 def cpu_reference(args, steps, sample_grid):
-    """The C oracle (reference algorithm restated, float64, all cores) on a bounded sample."""
+    """The reference's generated Cython kernel (oracle/_ref) on all host cores,
+    one x-slab per process; the C oracle when that module is absent."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    from oracle import OracleSimulation
-    from pylbm_gb300 import workloads as W
+    import ref_baseline
 
-    cores = os.cpu_count() or 1
-    o = OracleSimulation(W.tgv3d(n=sample_grid), nthreads=cores)
-    o.initialize()
-    o.one_time_step()  # warm-up
-    t0 = time.perf_counter()
-    o.run(steps)
-    dt = time.perf_counter() - t0
-    mlups = sample_grid ** 3 * steps / dt / 1e6
-    return {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "port",
-            "sample": f"D3Q19 TGV {sample_grid}^3, {steps} steps, float64, C oracle with OpenMP over {cores} threads"}
+    return ref_baseline.cpu_baseline(n=sample_grid, steps=steps)
 
 
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
-    base = cpu_reference(args, steps=max(args.steps // 10, 2), sample_grid=args.cpu_grid)
+    steps = max(min(args.steps, 40), 2)
+    base = cpu_reference(args, steps=steps, sample_grid=args.cpu_grid)
     line = {"impl": "reference", "metric": "MLUPS", "value": base["value"], "unit": "MLUPS", "n_gpus": world,
-            "steps": max(args.steps // 10, 2), "warmup": args.warmup, "higher_is_better": True,
+            "steps": steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "D3Q19 MRT periodic Taylor-Green vortex (sample of the 256^3 grid)",
                        "grid": [args.cpu_grid] * 3},
@@ -186,7 +184,7 @@ def main():
     ap.add_argument("--n", type=int, default=256, help="grid size per axis")
     ap.add_argument("--dtype", default="float32", choices=list(BYTES_PER_VALUE))
     ap.add_argument("--cpu-grid", type=int, default=256)
-    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-variants", action="store_true")

@@ -78,3 +78,26 @@ def test_planted_error_is_detected():
     o = OracleSimulation(d)
     o.run(50)
     assert rel_err(o.moments(), g["m50"]).max() > 1e-6
+
+
+def test_reference_kernel_baseline_computes_the_step():
+    """The CPU baseline's reference kernel (pylbm's generated one_time_step) agrees with the oracle."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle"))
+    import build_ref
+    import ref_baseline
+    mod = build_ref.load("tgv3d")
+    if mod is None:
+        pytest.skip("oracle/_ref not generated (needs the reference sources and Cython)")
+    n = 12
+    f = ref_baseline._slab_state(n, 0, n)
+    fnew = np.empty_like(f)
+    for _ in range(3):
+        ref_baseline._halo(f)
+        mod.one_time_step(f, fnew, *f.shape[:3])
+        f, fnew = fnew, f
+    o = OracleSimulation(W.tgv3d(n=n))
+    o.run(3)
+    got = np.moveaxis(f, -1, 0)[:, 1:-1, 1:-1, 1:-1]
+    assert np.abs(got - o.f[:, 1:-1, 1:-1, 1:-1]).max() < 1e-13
