@@ -81,6 +81,8 @@ int lbm_lattice_init(lbm_lattice* lat, int32_t dim, int32_t nv, int32_t dtype,
                      const int32_t* n, const int32_t* halo);
 
 int lbm_device_count(int32_t* count);
+/* Multiprocessor count and name of the current device (name NUL-terminated). */
+int lbm_device_info(int32_t* sm_count, char* name, int32_t name_len);
 int lbm_set_device(int32_t device);
 int lbm_device_synchronize(void);
 
@@ -165,6 +167,28 @@ int lbm_population_sums_noalloc(const void* f, const lbm_lattice* lat, double* s
 size_t lbm_population_sums_noalloc_max_bytes(void);
 
 /* ------------------------------------------------------------------ */
+/* Learned collision closure (no reference counterpart): a per-node    */
+/* MLP x(16, 9 used) -> 64 SiLU -> 64 SiLU -> y(8, 6 used) evaluated on */
+/* the tensor cores with BF16 operands and FP32 accumulation.           */
+/* params: FP32 block of lbm_mlp_sizes().nparam floats                  */
+/*   W1[64][16] b1[64] W2[64][64] b2[64] W3[8][64] b3[8]  (out x in);   */
+/* wbf16: the BF16 copies the kernels read (lbm_mlp_sync_weights).      */
+/* x: BF16 [n][16]; y, target: FP32 [n][8]; n a multiple of 16.         */
+/* ------------------------------------------------------------------ */
+int lbm_mlp_sizes(int32_t* nparam, int32_t* nweights_bf16);
+int lbm_mlp_scratch_bytes(int32_t n, size_t* bytes);
+int lbm_mlp_sync_weights(const float* params, void* wbf16, void* stream);
+int lbm_mlp_forward(const void* x, int32_t n, const void* wbf16, const float* params, float* y, void* stream);
+/* Adds dLoss/dparams to grad (FP32 atomics; zero it first) for the loss
+ * mean over samples and the 6 used outputs of (y - target)^2; writes the
+ * loss to *loss (device).  scratch: lbm_mlp_scratch_bytes(n) bytes. */
+int lbm_mlp_gradients(const void* x, const float* target, int32_t n, const void* wbf16, const float* params,
+                      float* grad, float* loss, void* scratch, size_t scratch_bytes, void* stream);
+/* Adam update of params (moments m, v), zeroes grad, refreshes wbf16. */
+int lbm_mlp_adam(float* params, float* m, float* v, float* grad, float lr, float beta1, float beta2, float eps,
+                 int32_t step, void* wbf16, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* lbm_scheme_<id>.so: per-scheme module (generated constants + the     */
 /* kernel templates of pylbm_gb300/csrc/scheme_kernels.cuh)            */
 /* ------------------------------------------------------------------ */
@@ -209,6 +233,39 @@ int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void*
 
 /* Moment-space relaxation m <- m + s (m_eq - m) (pylbm/algorithm/base.py:404-437). */
 int lbm_relaxation(double* m, const lbm_lattice* mlat, const double* prm, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Batched ensembles: many independent periodic simulations of one    */
+/* scheme, each with its own grid size and run-time parameters, in one */
+/* persistent launch per step.  No reference counterpart (pylbm runs   */
+/* one simulation per process).                                        */
+/* ------------------------------------------------------------------ */
+
+#define LBM_MAX_PRM 8
+
+typedef struct lbm_instance {
+  int64_t offset[2];          /* element offsets of the two population buffers in the arena */
+  int32_t n[3];               /* interior nodes per axis (1 beyond dim) */
+  int32_t halo[3];            /* ghost layers per axis */
+  int64_t stride[3];          /* as in lbm_lattice */
+  int64_t vstride;
+  int64_t origin;
+  int32_t rows;               /* interior rows: product of n over all axes but the last */
+  int32_t col_tiles;          /* tiles across the last axis: ceil(n_last / block) */
+  int32_t tile_begin;         /* index of this instance's first tile */
+  int32_t reserved;
+  double prm[LBM_MAX_PRM];    /* run-time parameters of this instance */
+} lbm_instance;
+
+/* One periodic step of every instance.  `arena` holds all populations (the
+ * storage type of the module), `inst` (device, ninst entries) describes them
+ * and `tile_instance` (device, ntiles entries) maps each tile to its
+ * instance; a tile is `rows_per_tile` rows x `block` consecutive nodes of the
+ * last axis.  `parity` selects which of the two buffers is read (then the
+ * other is written).  `grid` blocks of `block` threads stride over the tiles
+ * (grid = 0: one block per tile). */
+int lbm_ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
+                      int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream);
 
 #ifdef __cplusplus
 }

@@ -291,6 +291,21 @@ int lbm_device_count(int32_t* count) {
   return rc;
 }
 
+int lbm_device_info(int32_t* sm_count, char* name, int32_t name_len) {
+  int dev = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  cudaDeviceProp prop;
+  rc = cuda_check(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+  if (rc) return rc;
+  if (sm_count) *sm_count = prop.multiProcessorCount;
+  if (name && name_len > 0) {
+    std::strncpy(name, prop.name, (size_t)name_len - 1);
+    name[name_len - 1] = '\0';
+  }
+  return LBM_OK;
+}
+
 int lbm_set_device(int32_t device) { return cuda_check(cudaSetDevice(device), "cudaSetDevice"); }
 
 int lbm_device_synchronize(void) { return cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize"); }

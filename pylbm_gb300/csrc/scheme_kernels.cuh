@@ -133,6 +133,70 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_step_periodic(const S* __restrict
   for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * a.g.vstride, g[k]);
 }
 
+// Ensemble step: blocks stride over a tile list that covers every instance;
+// a tile is rows_per_tile rows x blockDim.x nodes of the last axis of one
+// instance.  The per-node work is the periodic step above with the
+// instance's own geometry and run-time parameters.
+__global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, const lbm_instance* __restrict__ inst,
+                                                         const int* __restrict__ tile_inst, int ntiles,
+                                                         int rows_per_tile, int parity) {
+  constexpr int L = LBM_DIM - 1;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const lbm_instance* I = inst + tile_inst[tile];
+    const int local = tile - I->tile_begin;
+    const int rt = local / I->col_tiles;
+    const int ct = local - rt * I->col_tiles;
+    const int col = ct * blockDim.x + threadIdx.x;
+    const int nL = I->n[L];
+    if (col >= nL) continue;
+    Geo g;
+    g.dim = LBM_DIM;
+    g.nv = LBM_Q;
+    for (int d = 0; d < 3; ++d) {
+      g.n[d] = I->n[d];
+      g.h[d] = I->halo[d];
+      g.stride[d] = I->stride[d];
+    }
+    g.vstride = I->vstride;
+    g.origin = I->origin;
+    R prm[kPrm];
+#pragma unroll
+    for (int p = 0; p < kPrm; ++p) prm[p] = (R)I->prm[p < LBM_MAX_PRM ? p : 0];
+    const S* __restrict__ f = arena + I->offset[parity];
+    S* __restrict__ fnew = arena + I->offset[parity ^ 1];
+    const int r0 = rt * rows_per_tile;
+    const int r1 = min(I->rows, r0 + rows_per_tile);
+    for (int r = r0; r < r1; ++r) {
+      int idx[3] = {0, 0, 0};
+      int q = r;
+#pragma unroll
+      for (int d = L - 1; d >= 0; --d) {
+        idx[d] = q % g.n[d] + g.h[d];
+        q /= g.n[d];
+      }
+      idx[L] = col + g.h[L];
+      const int i0 = idx[0], i1 = idx[1], i2 = idx[2];
+      const long long o = lbm::node_offset(g, i0, i1, i2);
+      long long off0[2 * LBM_VMAX + 1], off1[2 * LBM_VMAX + 1], off2[2 * LBM_VMAX + 1];
+#pragma unroll
+      for (int s = -LBM_VMAX; s <= LBM_VMAX; ++s) {
+        off0[s + LBM_VMAX] = LBM_DIM > 0 ? wrap_off(i0, s, g.n[0], g.h[0], g.stride[0]) : 0;
+        off1[s + LBM_VMAX] = LBM_DIM > 1 ? wrap_off(i1, s, g.n[1], g.h[1], g.stride[1]) : 0;
+        off2[s + LBM_VMAX] = LBM_DIM > 2 ? wrap_off(i2, s, g.n[2], g.h[2], g.stride[2]) : 0;
+      }
+      R gv[LBM_Q];
+#define LBM_PULL_ENS(k, vx, vy, vz)                                                              \
+  gv[k] = (R)Store<S>::load(f + o + (long long)(k) * g.vstride + off0[(vx) + LBM_VMAX] +        \
+                            off1[(vy) + LBM_VMAX] + off2[(vz) + LBM_VMAX]);
+      LBM_FOR_EACH_V(LBM_PULL_ENS)
+#undef LBM_PULL_ENS
+      lbm_collide<R>(gv, prm);
+#pragma unroll
+      for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * g.vstride, gv[k]);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(LBM_BLOCK) k_transport(const S* __restrict__ f, S* __restrict__ fnew,
                                                          StepArgs a) {
   int i0, i1, i2;
@@ -344,6 +408,22 @@ int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void*
   MomentArgs a = make_moment_args(nullptr, mlat, prm);
   k_equilibrium<<<node_grid(*mlat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, a);
   return lbm::launch_check("lbm_equilibrium");
+}
+
+int lbm_ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
+                      int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream) {
+  using namespace lbm_scheme;
+  if (!arena || !inst || !tile_instance) return lbm::fail(LBM_ERR_ARG, "lbm_ensemble_step: NULL argument");
+  if (ntiles < 0 || rows_per_tile < 1 || block < 32 || block > 1024 || (block % 32) || grid < 0 ||
+      (parity != 0 && parity != 1))
+    return lbm::fail(LBM_ERR_ARG, "lbm_ensemble_step: ntiles=%d rows_per_tile=%d block=%d grid=%d parity=%d",
+                     ntiles, rows_per_tile, block, grid, parity);
+  if (LBM_NPRM > LBM_MAX_PRM) return lbm::fail(LBM_ERR_UNSUPPORTED, "lbm_ensemble_step: too many parameters");
+  if (ntiles == 0) return LBM_OK;
+  unsigned blocks = (unsigned)(grid > 0 ? (grid < ntiles ? grid : ntiles) : ntiles);
+  k_step_ensemble<<<blocks, block, 0, (cudaStream_t)stream>>>((S*)arena, inst, tile_instance, ntiles,
+                                                               rows_per_tile, parity);
+  return lbm::launch_check("lbm_ensemble_step");
 }
 
 int lbm_relaxation(double* m, const lbm_lattice* mlat, const double* prm, void* stream) {

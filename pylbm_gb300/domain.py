@@ -21,7 +21,14 @@ VALOUT = -1
 
 
 class Domain:
-    def __init__(self, dico, stencil=None):
+    """Lattice geometry of a dictionary.
+
+    ``with_flags=False`` builds only sizes, halo and coordinates (no
+    ``in_or_out``/``distance``/``flag`` arrays), enough for domains periodic
+    along every axis, whose ghost layers no boundary method writes.
+    """
+
+    def __init__(self, dico, stencil=None, with_flags=True):
         self.valin = VALIN
         self.valout = VALOUT
         self.dim = _box_dim(dico)
@@ -66,6 +73,11 @@ class Domain:
             self.coords_halo.append(np.linspace(self.bounds[k][0] - beg, self.bounds[k][1] + beg,
                                                 self.global_size[k] + 2 * h))
         self.coords = [c[int(h):-int(h)] for c, h in zip(self.coords_halo, self.halo)]
+        if not with_flags:
+            if self.elements or any(l != -1 for l in self.box_label):
+                raise ValueError("a domain without flags must be periodic along every axis")
+            self.in_or_out = self.distance = self.flag = None
+            return
 
         uv = self.stencil.unique_v
         nu = uv.shape[0]

@@ -56,6 +56,35 @@ class Lattice(ctypes.Structure):
     ]
 
 
+LBM_MAX_PRM = 8
+
+
+class Instance(ctypes.Structure):
+    """lbm_instance of include/lbm_gb300.h (one member of an ensemble)."""
+
+    _fields_ = [
+        ("offset", ctypes.c_int64 * 2),
+        ("n", ctypes.c_int32 * 3),
+        ("halo", ctypes.c_int32 * 3),
+        ("stride", ctypes.c_int64 * 3),
+        ("vstride", ctypes.c_int64),
+        ("origin", ctypes.c_int64),
+        ("rows", ctypes.c_int32),
+        ("col_tiles", ctypes.c_int32),
+        ("tile_begin", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("prm", ctypes.c_double * LBM_MAX_PRM),
+    ]
+
+
+def device_info():
+    """(multiprocessor count, device name) of the current device."""
+    sm = ctypes.c_int32()
+    name = ctypes.create_string_buffer(256)
+    check(core().lbm_device_info(ctypes.byref(sm), name, 256))
+    return sm.value, name.value.decode()
+
+
 def nvcc_path():
     for cand in (os.environ.get("NVCC"),
                  os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc"),
@@ -82,8 +111,9 @@ def _nvcc_shared(sources, out, extra=()):
 
 def build_core(force=False):
     out = os.path.join(LIB_DIR, CORE_NAME)
-    srcs = [os.path.join(CSRC, "lbm_core.cu")]
-    deps = srcs + [os.path.join(CSRC, "lbm_common.cuh"), os.path.join(INCLUDE, "lbm_gb300.h")]
+    srcs = [os.path.join(CSRC, "lbm_core.cu"), os.path.join(CSRC, "lbm_closure.cu")]
+    deps = srcs + [os.path.join(CSRC, f) for f in ("lbm_common.cuh", "lbm_mlp.cuh")] + \
+        [os.path.join(INCLUDE, "lbm_gb300.h")]
     if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
         return out
     return _nvcc_shared(srcs, out)
@@ -116,6 +146,7 @@ def core():
             _sig(lib, "lbm_lattice_init", I32, [LP, I32, I32, I32, P, P])
             _sig(lib, "lbm_device_count", I32, [ctypes.POINTER(I32)])
             _sig(lib, "lbm_set_device", I32, [I32])
+            _sig(lib, "lbm_device_info", I32, [ctypes.POINTER(I32), ctypes.c_char_p, I32])
             _sig(lib, "lbm_device_synchronize", I32, [])
             _sig(lib, "lbm_alloc", I32, [ctypes.POINTER(P), SZ])
             _sig(lib, "lbm_free", I32, [P])
@@ -142,6 +173,13 @@ def core():
             _sig(lib, "lbm_population_sums", I32, [P, LP, P, P, P, SZ, P])
             _sig(lib, "lbm_population_sums_noalloc", I32, [P, LP, P, P, P])
             _sig(lib, "lbm_population_sums_noalloc_max_bytes", SZ, [])
+            F32 = ctypes.c_float
+            _sig(lib, "lbm_mlp_sizes", I32, [ctypes.POINTER(I32), ctypes.POINTER(I32)])
+            _sig(lib, "lbm_mlp_scratch_bytes", I32, [I32, ctypes.POINTER(SZ)])
+            _sig(lib, "lbm_mlp_sync_weights", I32, [P, P, P])
+            _sig(lib, "lbm_mlp_forward", I32, [P, I32, P, P, P, P])
+            _sig(lib, "lbm_mlp_gradients", I32, [P, P, I32, P, P, P, P, P, SZ, P])
+            _sig(lib, "lbm_mlp_adam", I32, [P, P, P, P, F32, F32, F32, F32, I32, P, P])
             _core = lib
     return _core
 
@@ -316,6 +354,7 @@ class SchemeModule:
         _sig(lib, "lbm_m2f", I32, [P, LP, P, LP, P])
         _sig(lib, "lbm_equilibrium", I32, [P, LP, P, P])
         _sig(lib, "lbm_relaxation", I32, [P, LP, P, P])
+        _sig(lib, "lbm_ensemble_step", I32, [P, P, P, I32, I32, I32, I32, I32, P])
 
     def call(self, rc):
         check(rc, self.lib, "lbm_scheme_last_error")

@@ -116,7 +116,11 @@ class Simulation:
         self.parity = bool(parity)
         self.dico = dico
         self.scheme = Scheme(dico)
-        self.domain = Domain(dico, self.scheme.stencil)
+        lab = dico["box"].get("label", -1)
+        lab = [lab] if isinstance(lab, (int, np.integer)) else list(lab)
+        all_periodic = all(int(l) == -1 for l in lab) and not dico.get("elements")
+        # wall distances and flags only matter where some boundary method needs them
+        self.domain = Domain(dico, self.scheme.stencil, with_flags=not all_periodic)
         if self.domain.dim != self.scheme.dim:
             raise ValueError("the dimension of the domain and of the scheme are not the same")
         self.dim = self.domain.dim
@@ -165,13 +169,22 @@ class Simulation:
     def extra_parameters_str(self):
         return {str(k): v for k, v in self.extra_parameters.items()}
 
-    def _prm(self):
+    def _prm(self, for_init=False):
+        """Run-time parameter vector (free symbols of the scheme, sorted by name).
+
+        Initialisation only evaluates the equilibrium, so it needs only the
+        symbols that appear there (as pylbm, which takes ``extra_parameters``
+        after construction); a step needs them all.
+        """
         vals = self.extra_parameters_str()
         names = [str(s) for s in self.scheme.free_symbols]
-        missing = [n for n in names if n not in vals]
+        needed = set(names)
+        if for_init:
+            needed = {str(s) for e in self.scheme.EQ for s in e.free_symbols} & needed
+        missing = [n for n in names if n not in vals and n in needed]
         if missing:
             raise ValueError(f"extra_parameters must give values for {missing}")
-        return np.array([float(vals[n]) for n in names] + [0.0], dtype=np.float64)
+        return np.array([float(vals.get(n, 0.0)) for n in names] + [0.0], dtype=np.float64)
 
     def feq_host(self, cons):
         """Equilibrium populations of boundary values on the host.
@@ -182,7 +195,7 @@ class Simulation:
         """
         params = self.extra_parameters_str()
         if self.module is not None and self.module.src.style == "reference":
-            prm = [float(params[str(s)]) for s in self.scheme.free_symbols]
+            prm = [float(params.get(str(s), 0.0)) for s in self.scheme.free_symbols]
             return self.module.src.reference_forms().feq_host(cons, prm)
         return self.scheme.feq_numpy(cons, params)
 
@@ -238,7 +251,7 @@ class Simulation:
             self._plane_view(plane, self._mlat)[...] = arr[c]
             mbuf.upload(plane, offset=c * self._mlat.vstride * 8, stream=self._stream)
         del arr
-        prm = self._prm()
+        prm = self._prm(for_init=True)
         pp = prm.ctypes.data_as(ctypes.c_void_p)
         if self.init_type == "moments":
             self.module.call(self.module.lib.lbm_equilibrium(mbuf.handle, ctypes.byref(self._mlat), pp, self._stream))

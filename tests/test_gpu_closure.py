@@ -1,0 +1,71 @@
+"""Learned-closure MLP kernels against the CPU oracle (oracle/mlp_oracle.py).
+
+Forward outputs and gradients of the BF16/FP32 tensor-core kernels are
+compared with a float64 NumPy evaluation that rounds to BF16 at the same
+points, and with the exact float64 gradient.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import mlp_oracle as mo
+from pylbm_gb300 import runtime
+from pylbm_gb300.closure import Mlp
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(n, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(n, mo.IN))
+    x[:, 9:] = 0.0
+    t = rng.normal(size=(n, mo.OUT))
+    return mo.bf16(x), t
+
+
+def test_forward_matches_oracle():
+    mlp = Mlp(seed=3)
+    x, _ = _data(256)
+    y = mlp.forward(x)
+    ref, _ = mo.forward(mlp.params_host().astype(np.float64), x)
+    assert np.abs(y - ref).max() <= 2e-3 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n", [16, 4096, 10000 - 10000 % 16])
+def test_gradients_match_oracle(n):
+    mlp = Mlp(seed=5)
+    x, t = _data(n, seed=n)
+    loss, grad = mlp.gradients(x, t)
+    p = mlp.params_host().astype(np.float64)
+    ref_loss, ref = mo.loss_and_grad(p, x, t, bf16_points=True)
+    _, exact = mo.loss_and_grad(p, x, t, bf16_points=False)
+    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    rel = np.linalg.norm(grad - ref) / np.linalg.norm(ref)
+    assert rel < 5e-3, rel
+    rel_exact = np.linalg.norm(grad - exact) / np.linalg.norm(exact)
+    assert rel_exact < 5e-2, rel_exact
+    # per-block agreement (each weight matrix and bias)
+    i = 0
+    for name, shape in mo.SHAPES:
+        k = int(np.prod(shape))
+        blk = slice(i, i + k)
+        if np.linalg.norm(ref[blk]) > 0:
+            assert np.linalg.norm(grad[blk] - ref[blk]) / np.linalg.norm(ref[blk]) < 2e-2, name
+        i += k
+
+
+def test_adam_training_reduces_loss():
+    """Fit a smooth map with the GPU training step; the loss must drop."""
+    rng = np.random.default_rng(7)
+    n = 8192
+    x = rng.normal(size=(n, mo.IN))
+    x[:, 9:] = 0.0
+    x = mo.bf16(x)
+    t = np.zeros((n, mo.OUT))
+    t[:, :6] = np.tanh(x[:, :6] * 0.7) + 0.3 * x[:, 1:7] * x[:, 2:8]
+    mlp = Mlp(seed=11)
+    first = mlp.train_step(x, t, lr=3e-3)
+    for _ in range(300):
+        last = mlp.train_step(x, t, lr=3e-3)
+    assert last < 0.2 * first, (first, last)

@@ -126,7 +126,8 @@ def test_core_library_builds_and_exports_header():
 
 def runtime_scheme_symbols():
     return {"lbm_one_time_step", "lbm_one_time_step_periodic", "lbm_transport", "lbm_f2m", "lbm_m2f",
-            "lbm_equilibrium", "lbm_relaxation", "lbm_scheme_last_error", "lbm_scheme_describe"}
+            "lbm_equilibrium", "lbm_relaxation", "lbm_scheme_last_error", "lbm_scheme_describe",
+            "lbm_ensemble_step"}
 
 
 def test_scheme_module_builds_and_exports_header():
@@ -208,3 +209,13 @@ def test_fast_and_reference_styles_share_constants():
     assert "0.666666666666667" in ref.header()
     with pytest.raises(SchemeError):
         SchemeSource(sc, shifted=True, c0=[1, 0, 0], style="reference")
+
+
+def test_periodic_domain_without_flags():
+    d = W.tgv3d(n=8)
+    dom = Domain(d, with_flags=False)
+    assert dom.flag is None and dom.shape_in == [8, 8, 8]
+    full = Domain(d)
+    assert [c.tolist() for c in dom.coords_halo] == [c.tolist() for c in full.coords_halo]
+    with pytest.raises(ValueError):
+        Domain(W.cavity(n=8), with_flags=False)

@@ -101,3 +101,27 @@ def test_reference_kernel_baseline_computes_the_step():
     o.run(3)
     got = np.moveaxis(f, -1, 0)[:, 1:-1, 1:-1, 1:-1]
     assert np.abs(got - o.f[:, 1:-1, 1:-1, 1:-1]).max() < 1e-13
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The MLP oracle's backward pass (float64, no rounding) against central differences."""
+    import mlp_oracle as mo
+    rng = np.random.default_rng(0)
+    p = mo.init_params(seed=1).astype(np.float64)
+    x = rng.normal(size=(48, mo.IN))
+    x[:, 9:] = 0.0
+    t = rng.normal(size=(48, mo.OUT))
+    _, g = mo.loss_and_grad(p, x, t, bf16_points=False)
+    idx = np.concatenate([rng.choice(mo.NPARAM, 40, replace=False), [mo.NPARAM - 1, mo.NPARAM - 3]])
+    fd = mo.finite_difference(p, x, t, idx)
+    assert np.allclose(g[idx], fd, rtol=1e-5, atol=1e-9)
+    # the two unused outputs carry no gradient
+    assert g[-2] == 0.0 and g[-1] == 0.0
+
+
+def test_mlp_oracle_bf16_rounding():
+    import mlp_oracle as mo
+    v = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9, 3.14159265, -2.71828])
+    r = mo.bf16(v)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125  # 1 + 2^-8 is a tie: to even
+    assert abs(r[3] - 3.140625) < 1e-12
