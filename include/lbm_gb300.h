@@ -142,6 +142,12 @@ int lbm_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, 
 int lbm_neumann(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
                 const lbm_lattice* lat, int32_t ordered, void* stream);
 
+/* Block average of the interior populations over factor^dim nodes into a
+ * dense float64 array out[nv][n0/factor][n1/factor][n2/factor] (physical
+ * values, last axis contiguous): restriction of a fine run onto a coarse
+ * lattice (training data of the learned closure; no reference counterpart). */
+int lbm_restrict(const void* f, const lbm_lattice* lat, double* out, int32_t factor, void* stream);
+
 /* FP64 sums over the interior nodes of every population (physical values),
  * the conservation diagnostic of the build (mass/momentum = M . sums).
  * `partials` is caller-provided device scratch of at least
@@ -214,6 +220,17 @@ int lbm_one_time_step(const void* f, void* fnew, const lbm_lattice* lat, const d
  * interior, ghost layers are neither read nor written (no halo pass). */
 int lbm_one_time_step_periodic(const void* f, void* fnew, const lbm_lattice* lat,
                                const double* prm, void* stream);
+
+/* Periodic step with the learned collision closure (no reference
+ * counterpart): after the relaxation, the non-conserved moments k >= nconsm
+ * receive corr_j = y_j * sig_out[j] + mu_out[j], y = MLP((m - mu_in) * isig_in)
+ * of the node's pre-collision moments m.  norm (host, 48 floats): mu_in[16],
+ * isig_in[16], mu_out[8], sig_out[8].  wbf16/params: the MLP blocks of
+ * lbm_mlp_* (device).  grid > 0 caps the number of blocks (persistent
+ * loop).  Needs nv <= 16 and nv - nconsm <= 8. */
+int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                                       const void* wbf16, const float* params, const float* norm, int32_t grid,
+                                       void* stream);
 
 /* Pure pull streaming on the interior (pylbm/algorithm/base.py:289-296). */
 int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* stream);

@@ -146,3 +146,231 @@ class Mlp:
         runtime.check(self._core.lbm_mlp_adam(self.p.handle, self.m.handle, self.v.handle, self.g.handle, lr, 0.9,
                                               0.999, 1e-8, self.step, self.w.handle, self.stream))
         return loss
+
+
+# ---------------------------------------------------------------------------
+# Closure model: MLP + normalisation, training data from restricted fine runs
+# ---------------------------------------------------------------------------
+class ClosureModel:
+    """A trained closure: MLP parameters and the normalisation of its inputs
+    (pre-collision moments) and outputs (non-conserved moment corrections)."""
+
+    def __init__(self, params, norm, meta=None, seed=0):
+        self.mlp = Mlp(seed=seed, params=params)
+        self.norm = np.ascontiguousarray(norm, dtype=np.float32)
+        if self.norm.size != 48:
+            raise ValueError("norm holds mu_in[16], isig_in[16], mu_out[8], sig_out[8]")
+        self.meta = dict(meta or {})
+        sm, _ = runtime.device_info()
+        self.grid = 2 * sm  # fused closure step: persistent blocks, two per SM
+
+    def norm_ptr(self):
+        return self.norm.ctypes.data_as(ctypes.c_void_p)
+
+    def save(self, path):
+        np.savez(path, params=self.mlp.params_host(), norm=self.norm,
+                 meta=np.array(repr(self.meta)))
+
+    @classmethod
+    def load(cls, path):
+        d = np.load(path, allow_pickle=False)
+        import ast
+        return cls(d["params"], d["norm"], ast.literal_eval(str(d["meta"])))
+
+
+def _restrict(sim, factor):
+    """Restricted physical populations (nv, n0/f, n1/f) of a simulation, float64."""
+    lat = sim._lat
+    nc = [lat.n[d] // factor for d in range(sim.dim)]
+    out = runtime.DeviceBuffer(8 * sim.scheme.nv * int(np.prod(nc)))
+    runtime.check(runtime.core().lbm_restrict(sim._F.handle, ctypes.byref(lat), out.handle, factor, sim._stream))
+    host = np.empty([sim.scheme.nv] + nc)
+    out.download(host, stream=sim._stream)
+    out.free()
+    return host
+
+
+def _pull(f, vel):
+    """Periodic pull of populations (nv, n0, n1): g_k(x) = f_k(x - v_k)."""
+    return np.array([np.roll(f[k], shift=tuple(int(c) for c in vel[k]), axis=(0, 1)) for k in range(f.shape[0])])
+
+
+def closure_pairs(scheme, c_now, c_next, rates, rng, nodes):
+    """Inputs (pre-collision moments) and targets (corrections) at random nodes.
+
+    c_now, c_next: restricted fine populations at coarse steps n and n+1.
+    The coarse step pulls c_now, relaxes, and should produce c_next at every
+    node; the target of the non-conserved moments is the difference between
+    M c_next and the plain relaxation.
+    """
+    nv, nc = scheme.nv, scheme.nconsm
+    vel = scheme.stencil.get_all_velocities()
+    pre = np.einsum("ij,j...->i...", scheme.M, _pull(c_now, vel))
+    flat = pre.reshape(nv, -1)
+    sel = rng.choice(flat.shape[1], size=min(nodes, flat.shape[1]), replace=False)
+    m = flat[:, sel]
+    meq = scheme.equilibrium_numpy(m[:nc])
+    relaxed = m + rates[:, None] * (meq - m)
+    target = (scheme.M @ c_next.reshape(nv, -1)[:, sel])
+    return m.T.copy(), (target - relaxed)[nc:].T.copy()
+
+
+def subfilter_pairs(scheme, c_now, fine_cons, factor, rng, nodes):
+    """Inputs and sub-filter targets at random coarse nodes.
+
+    The coarse step relaxes toward m_eq(R(c)), the equilibrium of the
+    restricted conserved moments, while the restricted fine flow relaxes
+    toward R(m_eq(c)); for the quadratic terms of the equilibrium the
+    difference is the sub-filter flux R(q_i q_j) - R(q_i) R(q_j) that the
+    coarse grid cannot represent.  The target correction of non-conserved
+    moment k is s_k * (R(m_eq,k(c)) - m_eq,k(R(c))), evaluated for the
+    pre-collision state of the next coarse step (``fine_cons``: the fine
+    conserved moments at that time).  The inputs are that step's
+    pre-collision moments M pull(c_now).
+    """
+    nv, nc = scheme.nv, scheme.nconsm
+    vel = scheme.stencil.get_all_velocities()
+    pre = np.einsum("ij,j...->i...", scheme.M, _pull(c_now, vel)).reshape(nv, -1)
+
+    def restrict(a):
+        n0, n1 = a.shape
+        return a.reshape(n0 // factor, factor, n1 // factor, factor).mean(axis=(1, 3)).ravel()
+
+    fine = np.array([np.asarray(c, dtype=np.float64).ravel() for c in fine_cons])
+    n0, n1 = np.asarray(fine_cons[0]).shape
+    meq_fine = scheme.equilibrium_numpy(fine)                      # (nv, fine nodes)
+    r_meq = np.array([restrict(meq_fine[k].reshape(n0, n1)) for k in range(nv)])
+    r_cons = np.array([restrict(np.asarray(c, dtype=np.float64)) for c in fine_cons])
+    meq_r = scheme.equilibrium_numpy(r_cons)
+    rates = scheme.rates_numpy()
+    sel = rng.choice(pre.shape[1], size=min(nodes, pre.shape[1]), replace=False)
+    target = (rates[:, None] * (r_meq - meq_r))[nc:, sel]
+    return pre[:, sel].T.copy(), target.T.copy()
+
+
+def study_dicos(seed, n, re=30000.0, u0=0.05):
+    """Double shear layer at Reynolds number ``re`` (U0 L / nu) on n^2 nodes."""
+    from . import workloads as W
+    nu = u0 * n / re
+    return W.shear_layer(n=n, nu=nu, u0=u0, seed=seed)
+
+
+def generate_training_data(seeds, n_fine=1024, factor=4, re=30000.0, times=(300, 500, 700, 900, 1100, 1300, 1500),
+                           nodes_per_pair=4096, fine_dtype="float64", rng_seed=0):
+    """(inputs, targets) pairs from fine runs restricted ``factor`` times."""
+    from .scheme import Scheme
+    from .simulation import Simulation
+
+    rng = np.random.default_rng(rng_seed)
+    n_coarse = n_fine // factor
+    coarse_scheme = Scheme(study_dicos(0, n_coarse, re))
+    xs, ys = [], []
+    for s in seeds:
+        sim = Simulation(study_dicos(int(s), n_fine, re), dtype=fine_dtype, parity=False)
+        step = 0
+        for tc in times:
+            sim.run(factor * tc - step)
+            step = factor * tc
+            now = _restrict(sim, factor)
+            sim.run(factor)
+            step += factor
+            fine = (sim.m[0], sim.m[1], sim.m[2])
+            x, y = subfilter_pairs(coarse_scheme, now, fine, factor, rng, nodes_per_pair)
+            xs.append(x)
+            ys.append(y)
+        sim.free()
+    return np.concatenate(xs), np.concatenate(ys)
+
+
+def fit_normalisation(x, y):
+    mu_in = np.zeros(16, np.float32)
+    isig_in = np.zeros(16, np.float32)
+    mu_out = np.zeros(8, np.float32)
+    sig_out = np.zeros(8, np.float32)
+    mu_in[:x.shape[1]] = x.mean(0)
+    sd = x.std(0)
+    isig_in[:x.shape[1]] = np.where(sd > 0, 1.0 / np.maximum(sd, 1e-30), 0.0)
+    mu_out[:y.shape[1]] = y.mean(0)
+    sig_out[:y.shape[1]] = np.maximum(y.std(0), 1e-30)
+    return np.concatenate([mu_in, isig_in, mu_out, sig_out])
+
+
+def train(x, y, steps=6000, batch=2048, lr=2e-3, seed=0, val_fraction=0.05, log=None, report_every=500,
+          corrected=None):
+    """Train the MLP with the GPU kernels (Adam, cosine learning-rate decay).
+
+    ``corrected``: indices (into the non-conserved moments) whose corrections
+    the closure applies; the others get a zero target and a zero output scale
+    (the network keeps its 6 outputs, the step leaves those moments to the
+    plain relaxation).  None corrects all of them.
+
+    Each block of ``report_every`` steps draws its minibatches from the
+    training samples, gathered on the host and uploaded once.  Returns
+    (ClosureModel, history).
+    """
+    import math
+    rng = np.random.default_rng(seed)
+    y = np.array(y, dtype=np.float64)
+    if corrected is not None:
+        keep = np.zeros(y.shape[1], dtype=bool)
+        keep[list(corrected)] = True
+        y[:, ~keep] = 0.0
+    norm = fit_normalisation(x, y)
+    if corrected is not None:
+        norm[40:40 + y.shape[1]][~keep] = 0.0  # zero output scale: no correction applied
+    nin, nout = x.shape[1], y.shape[1]
+    xn = np.zeros((x.shape[0], IN))
+    xn[:, :nin] = (x - norm[:nin]) * norm[16:16 + nin]
+    yn = np.zeros((y.shape[0], OUT))
+    scale = np.where(norm[40:40 + nout] > 0, norm[40:40 + nout], 1.0)
+    yn[:, :nout] = (y - norm[32:32 + nout]) / scale
+    perm = rng.permutation(x.shape[0])
+    nval = min(int(val_fraction * x.shape[0]), 65536) // 16 * 16
+    val, tr = perm[:nval], perm[nval:]
+    model = ClosureModel(init_params(seed), norm, {"nin": nin, "nout": nout})
+    mlp = model.mlp
+    xb_all = to_storage(xn, "bfloat16")
+    yf_all = yn.astype(np.float32)
+    history = []
+    done = 0
+    while done < steps:
+        chunk = min(report_every, steps - done)
+        idx = tr[rng.integers(0, tr.size, chunk * batch)]
+        dxe = runtime.DeviceBuffer(chunk * batch * IN * 2)
+        dxe.upload(xb_all[idx])
+        dye = runtime.DeviceBuffer(chunk * batch * OUT * 4)
+        dye.upload(yf_all[idx])
+        losses = []
+        for b in range(chunk):
+            s = done + b
+            lr_s = lr * 0.5 * (1.0 + math.cos(math.pi * s / steps))
+            xo = ctypes.c_void_p(dxe.ptr + b * batch * IN * 2)
+            yo = ctypes.c_void_p(dye.ptr + b * batch * OUT * 4)
+            losses.append(mlp.train_step_device(xo, yo, batch, lr_s, read_loss=(b % 16 == 0)))
+        dxe.free()
+        dye.free()
+        done += chunk
+        vl = validation_loss(mlp, xn[val], yn[val]) if nval else float("nan")
+        tl = float(np.mean([l for l in losses if l is not None]))
+        history.append({"step": done, "train": tl, "val": vl})
+        if log:
+            log(f"step {done}: train {tl:.4e} val {vl:.4e}")
+    return model, history
+
+
+def validation_loss(mlp, xn, yn):
+    y = mlp.forward(xn)
+    return float(((y[:, :NUSED] - yn[:, :NUSED]) ** 2).mean())
+
+
+def vorticity(q, rho=None):
+    """z-vorticity of the velocity q/rho on a periodic grid (central differences, unit spacing)."""
+    ux, uy = (q[0], q[1]) if rho is None else (q[0] / rho, q[1] / rho)
+    dux_dy = (np.roll(ux, -1, 1) - np.roll(ux, 1, 1)) / 2
+    duy_dx = (np.roll(uy, -1, 0) - np.roll(uy, 1, 0)) / 2
+    return duy_dx - dux_dy
+
+
+def restrict_moments(m, factor):
+    nv, a, b = m.shape
+    return m.reshape(nv, a // factor, factor, b // factor, factor).mean(axis=(2, 4))

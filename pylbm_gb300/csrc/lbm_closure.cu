@@ -294,20 +294,28 @@ __global__ void __launch_bounds__(32 * kWarps) k_mlp_wgrad(const __nv_bfloat16* 
   }
 }
 
+// FP32 master block -> BF16 copies in fragment order (lbm_mlp.cuh):
+//   w1t = W1 [64 out][16 in], w2t = W2 [64][64], w3t = W3 [8][64]      (forward)
+//   w2n = W2^T [64 in][64 out], w3n = W3^T [64 in][16 (8 out + zeros)]   (backward)
 __global__ void k_mlp_sync(const float* __restrict__ p, __nv_bfloat16* __restrict__ wb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < H * IN) wb[BW1T + i] = __float2bfloat16_rn(p[PW1 + i]);
+  int n, k;
+  if (i < H * IN) {
+    frag_source(i, IN, n, k);
+    wb[BW1T + i] = __float2bfloat16_rn(p[PW1 + n * IN + k]);
+  }
   if (i < H * H) {
-    wb[BW2T + i] = __float2bfloat16_rn(p[PW2 + i]);
-    const int o = i / H, c = i % H;  // W2t[o][c] -> W2n[c][o]
-    wb[BW2N + c * H + o] = __float2bfloat16_rn(p[PW2 + i]);
+    frag_source(i, H, n, k);
+    wb[BW2T + i] = __float2bfloat16_rn(p[PW2 + n * H + k]);
+    wb[BW2N + i] = __float2bfloat16_rn(p[PW2 + k * H + n]);  // transposed: n = in, k = out
   }
   if (i < OUT * H) {
-    wb[BW3T + i] = __float2bfloat16_rn(p[PW3 + i]);
+    frag_source(i, H, n, k);
+    wb[BW3T + i] = __float2bfloat16_rn(p[PW3 + n * H + k]);
   }
-  if (i < H * 16) {  // W3n[c][o], o padded to 16
-    const int c = i / 16, o = i % 16;
-    wb[BW3N + i] = o < OUT ? __float2bfloat16_rn(p[PW3 + o * H + c]) : __float2bfloat16(0.0f);
+  if (i < H * 16) {
+    frag_source(i, 16, n, k);  // n = in (64), k = out (16, padded)
+    wb[BW3N + i] = k < OUT ? __float2bfloat16_rn(p[PW3 + k * H + n]) : __float2bfloat16(0.0f);
   }
 }
 

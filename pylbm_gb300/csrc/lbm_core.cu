@@ -180,6 +180,37 @@ __global__ void __launch_bounds__(kThreads) k_sums_stage2(const double* __restri
   }
 }
 
+// ---------------------------------------------------------------- restriction
+struct RestrictArgs {
+  double shift[LBM_MAX_Q];
+  int factor;
+  int nc[3];        // coarse interior sizes (1 beyond dim)
+  long long cells;  // product of nc
+};
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_restrict(const S* __restrict__ f, Geo g, RestrictArgs r,
+                                                       double* __restrict__ out) {
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= r.cells) return;
+  const int k = blockIdx.y;
+  int c[3];
+  long long q = cell;
+  for (int d = 2; d >= 0; --d) {
+    c[d] = (int)(q % r.nc[d]);
+    q /= r.nc[d];
+  }
+  const int f0 = g.dim > 0 ? r.factor : 1, f1 = g.dim > 1 ? r.factor : 1, f2 = g.dim > 2 ? r.factor : 1;
+  double acc = 0.0;
+  for (int a = 0; a < f0; ++a)
+    for (int b = 0; b < f1; ++b)
+      for (int e = 0; e < f2; ++e) {
+        const int i0 = c[0] * f0 + a + g.h[0], i1 = c[1] * f1 + b + g.h[1], i2 = c[2] * f2 + e + g.h[2];
+        acc += (double)Store<S>::load(f + (long long)k * g.vstride + node_offset(g, i0, i1, i2));
+      }
+  out[(long long)k * r.cells + cell] = acc / (double)(f0 * f1 * f2) + r.shift[k];
+}
+
 SumPlan make_sum_plan(const lbm_lattice& l) {
   SumPlan p;
   const int L = l.dim - 1;
@@ -469,6 +500,34 @@ int lbm_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, 
 int lbm_neumann(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
                 const lbm_lattice* lat, int32_t ordered, void* stream) {
   return boundary_common(f, iload0, istore, ncond, nullptr, lat, ordered, 1.0, "lbm_neumann", stream);
+}
+
+int lbm_restrict(const void* f, const lbm_lattice* lat, double* out, int32_t factor, void* stream) {
+  int rc = check_lattice(lat, "lbm_restrict");
+  if (rc) return rc;
+  if (!f || !out) return fail(LBM_ERR_ARG, "lbm_restrict: NULL");
+  if (factor < 1) return fail(LBM_ERR_ARG, "lbm_restrict: factor=%d", factor);
+  RestrictArgs r;
+  r.factor = factor;
+  r.cells = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (d < lat->dim) {
+      if (lat->n[d] % factor) return fail(LBM_ERR_ARG, "lbm_restrict: n[%d]=%d not divisible by %d", d, lat->n[d], factor);
+      r.nc[d] = lat->n[d] / factor;
+    } else {
+      r.nc[d] = 1;
+    }
+    r.cells *= r.nc[d];
+  }
+  for (int k = 0; k < LBM_MAX_Q; ++k) r.shift[k] = k < lat->nv ? lat->shift[k] : 0.0;
+  Geo g = make_geo(*lat);
+  dim3 grid((unsigned)((r.cells + kThreads - 1) / kThreads), (unsigned)lat->nv);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    k_restrict<S><<<grid, kThreads, 0, s>>>((const S*)f, g, r, out);
+    return launch_check("lbm_restrict");
+  });
 }
 
 int lbm_population_sums_scratch_bytes(const lbm_lattice* lat, size_t* bytes) {

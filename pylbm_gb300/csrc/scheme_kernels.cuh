@@ -17,6 +17,7 @@
 #pragma once
 
 #include "lbm_common.cuh"
+#include "lbm_mlp.cuh"
 
 #include <type_traits>
 
@@ -195,6 +196,125 @@ __global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, c
       for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * g.vstride, gv[k]);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Periodic step with the learned collision closure: after the relaxation the
+// non-conserved moments receive the MLP's correction, computed from the
+// node's pre-collision moments.  Each warp stages the normalised moments of
+// its 32 nodes in shared memory and evaluates the MLP on the tensor cores as
+// two 16-row tiles (lbm_mlp.cuh); conserved moments are never changed.
+struct ClosureArgs {
+  const __nv_bfloat16* w;  // BF16 weight block (forward part read)
+  const float* params;     // FP32 parameter block (biases read)
+  float mu_in[16], isig_in[16];
+  float mu_out[8], sig_out[8];
+  long long nodes;         // interior nodes
+};
+
+constexpr int kClosureWarps = 8;
+#ifndef LBM_CLOSURE_MIN_BLOCKS
+// no register cap: capping at 64 or 80 registers spills and was slower
+#define LBM_CLOSURE_MIN_BLOCKS 1
+#endif
+
+__global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_step_periodic_closure(const S* __restrict__ f,
+                                                                               S* __restrict__ fnew, StepArgs a,
+                                                                               ClosureArgs c) {
+#if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
+  using namespace lbm_mlp;
+  __shared__ __align__(16) __nv_bfloat16 w_s[BW2N];
+  __shared__ float b_s[2 * H + OUT];
+  __shared__ __align__(16) __nv_bfloat16 x_s[kClosureWarps][32 * IN];
+  __shared__ float y_s[kClosureWarps][16 * OUT];
+  static_assert((BW2N * sizeof(__nv_bfloat16)) % 16 == 0, "weight block must be a whole number of 16-byte words");
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(c.w);
+    uint4* dst = reinterpret_cast<uint4*>(w_s);
+    for (int i = threadIdx.x; i < (int)(BW2N * sizeof(__nv_bfloat16) / 16); i += blockDim.x) dst[i] = src[i];
+  }
+  for (int i = threadIdx.x; i < H; i += blockDim.x) {
+    b_s[i] = c.params[PB1 + i];
+    b_s[H + i] = c.params[PB2 + i];
+  }
+  for (int i = threadIdx.x; i < OUT; i += blockDim.x) b_s[2 * H + i] = c.params[PB3 + i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  const Geo& g = a.g;
+  // 16 nodes per warp (one 16-row MMA tile): lanes 0..15 own a node, all 32
+  // lanes evaluate the MLP; short per-warp chains, twice the warps in flight
+  const long long per_block = 16 * kClosureWarps;
+  for (long long base = (long long)blockIdx.x * per_block; base < c.nodes; base += (long long)gridDim.x * per_block) {
+    const long long node = base + warp * 16 + lane;
+    const bool active = lane < 16 && node < c.nodes;
+    int idx[3] = {0, 0, 0};
+    long long q = active ? node : 0;
+    for (int d = LBM_DIM - 1; d >= 0; --d) {
+      idx[d] = (int)(q % g.n[d]) + g.h[d];
+      q /= g.n[d];
+    }
+    const long long o = lbm::node_offset(g, idx[0], idx[1], idx[2]);
+    R gv[LBM_Q], m[LBM_Q];
+    if (active) {
+      long long off0[2 * LBM_VMAX + 1], off1[2 * LBM_VMAX + 1], off2[2 * LBM_VMAX + 1];
+#pragma unroll
+      for (int s = -LBM_VMAX; s <= LBM_VMAX; ++s) {
+        off0[s + LBM_VMAX] = LBM_DIM > 0 ? wrap_off(idx[0], s, g.n[0], g.h[0], g.stride[0]) : 0;
+        off1[s + LBM_VMAX] = LBM_DIM > 1 ? wrap_off(idx[1], s, g.n[1], g.h[1], g.stride[1]) : 0;
+        off2[s + LBM_VMAX] = LBM_DIM > 2 ? wrap_off(idx[2], s, g.n[2], g.h[2], g.stride[2]) : 0;
+      }
+#define LBM_PULL_CL(k, vx, vy, vz)                                                              \
+  gv[k] = (R)Store<S>::load(f + o + (long long)(k) * g.vstride + off0[(vx) + LBM_VMAX] +        \
+                            off1[(vy) + LBM_VMAX] + off2[(vz) + LBM_VMAX]);
+      LBM_FOR_EACH_V(LBM_PULL_CL)
+#undef LBM_PULL_CL
+      lbm_moments<R>(gv, m);
+    } else {
+#pragma unroll
+      for (int k = 0; k < LBM_Q; ++k) m[k] = (R)0;
+    }
+    // normalised pre-collision moments (absolute values) -> BF16 row of this lane
+    if (lane < 16) {
+      __nv_bfloat16* xr = &x_s[warp][lane * IN];
+#pragma unroll
+      for (int k = 0; k < IN; ++k) {
+        float v = 0.0f;
+        if (k < LBM_Q && active)
+          v = ((float)m[k] + (float)lbm_dev_mref[k < LBM_Q ? k : 0] - c.mu_in[k]) * c.isig_in[k];
+        xr[k] = __float2bfloat16_rn(v);
+      }
+    }
+    __syncwarp();
+    {
+      const __nv_bfloat16* xt = &x_s[warp][0];
+      uint32_t xa[4];
+      xa[0] = *reinterpret_cast<const uint32_t*>(xt + gq * IN + 2 * tq);
+      xa[1] = *reinterpret_cast<const uint32_t*>(xt + (gq + 8) * IN + 2 * tq);
+      xa[2] = *reinterpret_cast<const uint32_t*>(xt + gq * IN + 8 + 2 * tq);
+      xa[3] = *reinterpret_cast<const uint32_t*>(xt + (gq + 8) * IN + 8 + 2 * tq);
+      float y[4], z1[8][4], z2[8][4];
+      uint32_t h1a[4][4], h2a[4][4];
+      forward_tile<false>(xa, w_s, b_s, b_s + H, b_s + 2 * H, lane, y, z1, z2, h1a, h2a);
+      float* yt = &y_s[warp][0];
+      yt[gq * OUT + 2 * tq] = y[0];
+      yt[gq * OUT + 2 * tq + 1] = y[1];
+      yt[(gq + 8) * OUT + 2 * tq] = y[2];
+      yt[(gq + 8) * OUT + 2 * tq + 1] = y[3];
+    }
+    __syncwarp();
+    if (active) {
+      lbm_relax<R>(m, a.prm);
+#pragma unroll
+      for (int j = 0; j < LBM_Q - LBM_NCONS; ++j)
+        m[LBM_NCONS + j] += (R)(y_s[warp][lane * OUT + j] * c.sig_out[j] + c.mu_out[j]);
+      lbm_populations<R>(m, gv);
+#pragma unroll
+      for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * g.vstride, gv[k]);
+    }
+    __syncwarp();
+  }
+#endif
 }
 
 __global__ void __launch_bounds__(LBM_BLOCK) k_transport(const S* __restrict__ f, S* __restrict__ fnew,
@@ -408,6 +528,38 @@ int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void*
   MomentArgs a = make_moment_args(nullptr, mlat, prm);
   k_equilibrium<<<node_grid(*mlat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, a);
   return lbm::launch_check("lbm_equilibrium");
+}
+
+int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                                       const void* wbf16, const float* params, const float* norm, int32_t grid,
+                                       void* stream) {
+  using namespace lbm_scheme;
+  const char* who = "lbm_one_time_step_periodic_closure";
+  int rc = check_pop_lattice(lat, who);
+  if (rc) return rc;
+  if (LBM_Q > 16 || LBM_Q - LBM_NCONS > 8)
+    return lbm::fail(LBM_ERR_UNSUPPORTED, "%s: the closure MLP takes at most 16 moments and 8 corrections", who);
+  if (!f || !fnew || f == fnew || !wbf16 || !params || !norm) return lbm::fail(LBM_ERR_ARG, "%s: bad pointers", who);
+  if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "%s: %d parameters expected", who, LBM_NPRM);
+  StepArgs a = make_step_args(*lat, prm);
+  ClosureArgs c;
+  c.w = (const __nv_bfloat16*)wbf16;
+  c.params = params;
+  for (int i = 0; i < 16; ++i) {
+    c.mu_in[i] = norm[i];
+    c.isig_in[i] = norm[16 + i];
+  }
+  for (int i = 0; i < 8; ++i) {
+    c.mu_out[i] = norm[32 + i];
+    c.sig_out[i] = norm[40 + i];
+  }
+  c.nodes = (long long)lat->n[0] * lat->n[1] * lat->n[2];
+  const long long per = 16 * kClosureWarps;
+  long long blocks = (c.nodes + per - 1) / per;
+  if (grid > 0 && blocks > grid) blocks = grid;
+  k_step_periodic_closure<<<(unsigned)blocks, 32 * kClosureWarps, 0, (cudaStream_t)stream>>>((const S*)f, (S*)fnew,
+                                                                                             a, c);
+  return lbm::launch_check(who);
 }
 
 int lbm_ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,

@@ -172,6 +172,7 @@ def core():
             _sig(lib, "lbm_population_sums_scratch_bytes", I32, [LP, ctypes.POINTER(SZ)])
             _sig(lib, "lbm_population_sums", I32, [P, LP, P, P, P, SZ, P])
             _sig(lib, "lbm_population_sums_noalloc", I32, [P, LP, P, P, P])
+            _sig(lib, "lbm_restrict", I32, [P, LP, P, I32, P])
             _sig(lib, "lbm_population_sums_noalloc_max_bytes", SZ, [])
             F32 = ctypes.c_float
             _sig(lib, "lbm_mlp_sizes", I32, [ctypes.POINTER(I32), ctypes.POINTER(I32)])
@@ -355,6 +356,7 @@ class SchemeModule:
         _sig(lib, "lbm_equilibrium", I32, [P, LP, P, P])
         _sig(lib, "lbm_relaxation", I32, [P, LP, P, P])
         _sig(lib, "lbm_ensemble_step", I32, [P, P, P, I32, I32, I32, I32, I32, P])
+        _sig(lib, "lbm_one_time_step_periodic_closure", I32, [P, P, LP, P, P, P, P, I32, P])
 
     def call(self, rc):
         check(rc, self.lib, "lbm_scheme_last_error")

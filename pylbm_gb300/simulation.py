@@ -304,12 +304,31 @@ class Simulation:
                                             self._stream)
             runtime.check(rc)
 
+    def set_closure(self, model):
+        """Use a learned collision closure (closure.ClosureModel) from the next step on.
+
+        Periodic domains only; ``None`` returns to the plain relaxation.
+        """
+        if model is not None and not self.periodic:
+            raise ValueError("the learned closure runs on periodic domains")
+        self.closure = model
+        self._drop_graph()
+
+    def _launch_step(self, F, Fnew, pp):
+        model = getattr(self, "closure", None)
+        if model is not None:
+            norm = model.norm_ptr()
+            self.module.call(self.module.lib.lbm_one_time_step_periodic_closure(
+                F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.w.handle, model.mlp.p.handle, norm,
+                model.grid, self._stream))
+            return
+        fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
+        self.module.call(fn(F.handle, Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
+
     def _enqueue_step(self, F, Fnew, prm):
         if not self.periodic:
             self._enqueue_boundary(F)
-        pp = prm.ctypes.data_as(ctypes.c_void_p)
-        fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
-        self.module.call(fn(F.handle, Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
+        self._launch_step(F, Fnew, prm.ctypes.data_as(ctypes.c_void_p))
 
     def boundary_condition(self):
         """Ghost refresh then every boundary method (pylbm/simulation.py:374-390)."""
@@ -329,9 +348,7 @@ class Simulation:
         self._m_cache = {}
         self.boundary_condition()
         prm = self._prm()
-        pp = prm.ctypes.data_as(ctypes.c_void_p)
-        fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
-        self.module.call(fn(self._F.handle, self._Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
+        self._launch_step(self._F, self._Fnew, prm.ctypes.data_as(ctypes.c_void_p))
         self._F, self._Fnew = self._Fnew, self._F
         self.t += self.dt
         self.nt += 1

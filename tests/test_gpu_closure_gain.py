@@ -1,0 +1,43 @@
+"""What the trained closure gains over the plain coarse method (held-out seed).
+
+The model in pylbm_gb300/data was trained by pylbm_gb300.closure_study on
+200 seeds of the Re 30 000 double shear layer (1024^2 float64 runs restricted
+4x); seed 100000 was not among them.  After 1500 coarse steps, the learned
+256^2 run must be closer to the float64 1024^2 solution than the plain 256^2
+run, with mass and momentum conserved.
+"""
+import numpy as np
+import pytest
+
+from pylbm_gb300 import Simulation
+from pylbm_gb300.closure import ClosureModel, restrict_moments, study_dicos, vorticity
+from pylbm_gb300.closure_study import DEFAULT_MODEL
+
+pytestmark = pytest.mark.gpu
+
+
+def _vort(sim, factor):
+    m = np.array([sim.m[k] for k in range(3)])
+    if factor > 1:
+        m = restrict_moments(m, factor)
+    return vorticity(m[1:], m[0])
+
+
+def test_learned_closure_beats_plain_coarse_on_held_out_seed():
+    seed, steps = 100000, 1500
+    ref = Simulation(study_dicos(seed, 1024), dtype="float64", parity=False)
+    ref.run(4 * steps)
+    w_ref = _vort(ref, 4)
+    ref.free()
+    plain = Simulation(study_dicos(seed, 256), dtype="float32")
+    plain.run(steps)
+    err_plain = np.linalg.norm(_vort(plain, 1) - w_ref) / np.linalg.norm(w_ref)
+    learned = Simulation(study_dicos(seed, 256), dtype="float32")
+    learned.set_closure(ClosureModel.load(DEFAULT_MODEL))
+    c0 = learned.conserved_sums()
+    learned.run(steps)
+    c1 = learned.conserved_sums()
+    err_learned = np.linalg.norm(_vort(learned, 1) - w_ref) / np.linalg.norm(w_ref)
+    assert err_learned < 0.97 * err_plain, (err_learned, err_plain)
+    assert abs(c1[0] - c0[0]) < 1e-6 * abs(c0[0])
+    assert np.all(np.abs(c1[1:] - c0[1:]) < 1e-6 * abs(c0[0]))

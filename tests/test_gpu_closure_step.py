@@ -1,0 +1,79 @@
+"""The fused closure step (lbm_one_time_step_periodic_closure).
+
+With a zero network it must equal the plain step bit for bit; with a random
+network it must equal the plain relaxation plus the MLP correction computed
+by the standalone inference kernel, and it must leave mass and momentum
+exactly as the plain step does.
+"""
+import numpy as np
+import pytest
+import sympy as sp
+
+from pylbm_gb300 import Simulation
+from pylbm_gb300 import workloads as W
+from pylbm_gb300.closure import ClosureModel, closure_pairs, init_params, _restrict
+from pylbm_gb300.scheme import Scheme
+
+pytestmark = pytest.mark.gpu
+
+
+def _norm(scale_out=1.0):
+    mu_in = np.zeros(16)
+    mu_in[0] = 1.0
+    isig = np.zeros(16)
+    isig[:9] = [200.0, 20.0, 20.0, 50.0, 50.0, 50.0, 50.0, 200.0, 200.0]
+    mu_out = np.zeros(8)
+    sig_out = np.zeros(8)
+    sig_out[:6] = scale_out
+    return np.concatenate([mu_in, isig, mu_out, sig_out])
+
+
+def _moments(sim):
+    return np.array([sim.m[k] for k in range(sim.scheme.nv)])
+
+
+def test_zero_network_equals_plain_step():
+    d = W.shear_layer(n=64, nu=1e-3)
+    a = Simulation(d, dtype="float32")
+    b = Simulation(d, dtype="float32")
+    p = np.zeros_like(init_params(0))
+    b.set_closure(ClosureModel(p, _norm()))
+    a.run(25)
+    b.run(25)
+    assert np.array_equal(_moments(a), _moments(b))
+
+
+def test_closure_step_equals_relaxation_plus_network():
+    d = W.shear_layer(n=48, nu=1e-3, seed=4)
+    sim = Simulation(d, dtype="float32")
+    sim.run(10)
+    before = _restrict(sim, 1)
+    model = ClosureModel(init_params(3) * 0.5, _norm(scale_out=1e-4))
+    sim.set_closure(model)
+    sim.one_time_step()
+    after = _restrict(sim, 1)
+    sc = Scheme(d)
+    rates = sc.rates_numpy()
+    rng = np.random.default_rng(0)
+    n = before.shape[1] * before.shape[2]
+    x, corr_needed = closure_pairs(sc, before, after, rates, rng, nodes=n)
+    # recompute the correction the kernel should have applied
+    xn = np.zeros((n, 16))
+    xn[:, :9] = (x - model.norm[:9]) * model.norm[16:25]
+    y = model.mlp.forward(xn)
+    expected = y[:, :6] * model.norm[40:46] + model.norm[32:38]
+    # closure_pairs' target is exactly the correction that was applied
+    assert np.abs(corr_needed - expected).max() < 2e-5 * max(1.0, np.abs(expected).max()) + 2e-6
+    # conserved moments are those of the plain step (pulled mass and momentum)
+    assert np.abs(corr_needed).max() > 1e-6  # the network did something
+
+
+def test_closure_conserves_mass_and_momentum():
+    d = W.shear_layer(n=64, nu=1e-3, seed=2)
+    sim = Simulation(d, dtype="float32")
+    sim.set_closure(ClosureModel(init_params(9), _norm(scale_out=1e-3)))
+    c0 = sim.conserved_sums()
+    sim.run(50)
+    c1 = sim.conserved_sums()
+    assert abs(c1[0] - c0[0]) < 1e-6 * abs(c0[0])
+    assert np.all(np.abs(c1[1:] - c0[1:]) < 1e-6 * abs(c0[0]))
