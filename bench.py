@@ -135,6 +135,19 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def aggregate(ms, nodes, steps, world, dist=None):
+    """Whole-job rate of N replicas: the slowest rank's time, all ranks' nodes.
+
+    Returns (max ms over ranks, MLUPS = world * nodes * steps / max time).
+    """
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(ms)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, nodes * steps * world / (ms / 1e3) / 1e6
+
+
 def time_steps(sim, steps):
     """Device time (ms) of ``steps`` steps replayed from the captured graph."""
     from pylbm_gb300 import runtime
@@ -172,6 +185,56 @@ def variants(args):
         out[name] = {"MLUPS": mlups, "ms_per_step": ms / steps, "GB/s": gbs, "hbm_frac": gbs / peak,
                      "steps": steps}
         sim.free()
+    out["ensemble_512_d2q9_f16"] = ensemble_variant(peak)
+    out["learned_closure_d2q9"] = closure_variant()
+    return out
+
+
+def ensemble_variant(peak, steps=200):
+    """512 periodic double shear layers (sides 64..512, nu log-uniform), FP16 storage, one launch per step."""
+    from pylbm_gb300 import runtime
+    from pylbm_gb300.ensemble import shear_ensemble
+
+    t0 = time.perf_counter()
+    ens, sides, nus = shear_ensemble(count=512, seed=0, dtype="float16")
+    setup = time.perf_counter() - t0
+    ens.run(4)
+    ens.synchronize()
+    e0, e1 = runtime.Event(), runtime.Event()
+    e0.record(ens._stream)
+    ens.run(steps)
+    e1.record(ens._stream)
+    ms = e0.elapsed_ms(e1)
+    nodes = ens.total_nodes
+    res = {"MLUPS": nodes * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
+           "GB/s": 36 * nodes * steps / (ms / 1e3) / 1e9, "hbm_frac": 36 * nodes * steps / (ms / 1e3) / 1e9 / peak,
+           "instances": len(sides), "nodes_per_step": nodes, "tile": list(ens.tile), "setup_s": setup,
+           "steps": steps}
+    ens.free()
+    return res
+
+
+def closure_variant(steps=1500):
+    """Device time of the Re 30 000 shear layer: learned 256^2 vs plain 256^2 / 512^2 / 1024^2 (FP32)."""
+    from pylbm_gb300 import Simulation
+    from pylbm_gb300.closure import ClosureModel, study_dicos
+    from pylbm_gb300.closure_study import DEFAULT_MODEL
+
+    if not os.path.exists(DEFAULT_MODEL):
+        return {"unavailable": "no trained model"}
+    out = {}
+    model = ClosureModel.load(DEFAULT_MODEL)
+    for name, n, factor, mdl in (("plain_256", 256, 1, None), ("learned_256", 256, 1, model),
+                                 ("plain_512", 512, 2, None), ("plain_1024", 1024, 4, None)):
+        sim = Simulation(study_dicos(100000, n), dtype="float32")
+        if mdl is not None:
+            sim.set_closure(mdl)
+        ms = time_steps(sim, factor * steps)
+        out[name] = {"ms_total": ms, "us_per_step": 1e3 * ms / (factor * steps), "steps": factor * steps}
+        sim.free()
+    out["fine_over_learned_time"] = out["plain_1024"]["ms_total"] / out["learned_256"]["ms_total"]
+    out["note"] = ("same physical time; vorticity errors vs the FP64 1024^2 run come from "
+                   "python -m pylbm_gb300.closure_study (20 held-out seeds)")
     return out
 
 
@@ -229,13 +292,8 @@ def main():
     e1.record(sim._stream)
     ms = e0.elapsed_ms(e1)
     clocks = sampler.stop()
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = aggregate(ms, nodes, args.steps, world, dist)
     ms_step = ms / args.steps
-    value = nodes * args.steps * world / (ms / 1e3) / 1e6
     bpl = 2 * sim.scheme.nv * BYTES_PER_VALUE[args.dtype]
     achieved = bpl * nodes / (ms_step / 1e3) / 1e9
     peak, peak_src = measured_peaks()
