@@ -142,6 +142,29 @@ int lbm_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, 
 int lbm_neumann(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
                 const lbm_lattice* lat, int32_t ordered, void* stream);
 
+/* Bouzidi interpolated walls (second-order wall position from the link's
+ * wall distance).  iload1 is a second load list of the same layout and
+ * dist[c] the interpolation weight of link c (pylbm's BoundaryMethod.s:
+ * 2q for q < 1/2, 1/(2q) otherwise, pylbm/boundary.py:508-534).  With
+ * d = dist[c], f0 = f[iload0[c]], f1 = f[iload1[c]], evaluated in this order
+ * without fused multiply-adds as pylbm's generated code does:
+ *   bouzidi_bounce_back:       f[istore] = ((1-d) f1 + d f0) + rhs
+ *                              (pylbm/boundary.py:570-618; the loads read a
+ *                              copy of f taken before the method runs)
+ *   bouzidi_anti_bounce_back:  f[istore] = ((1-d) f1 - d f0) + rhs
+ *                              (pylbm/boundary.py:707-756; loads read f
+ *                              itself, links in list order)
+ * Bounce-back: `scratch` (ncond doubles, device) gives the copy semantics
+ * by computing every link before storing any; NULL is allowed when no link
+ * loads a population another link of the call stores.  Anti-bounce-back:
+ * `ordered` as for lbm_bounce_back. */
+int lbm_bouzidi_bounce_back(void* f, const int32_t* iload0, const int32_t* iload1, const int32_t* istore,
+                            int32_t ncond, const double* rhs, const double* dist, const lbm_lattice* lat,
+                            double* scratch, void* stream);
+int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* iload1, const int32_t* istore,
+                                 int32_t ncond, const double* rhs, const double* dist, const lbm_lattice* lat,
+                                 int32_t ordered, void* stream);
+
 /* Block average of the interior populations over factor^dim nodes into a
  * dense float64 array out[nv][n0/factor][n1/factor][n2/factor] (physical
  * values, last axis contiguous): restriction of a fine run onto a coarse
@@ -268,19 +291,28 @@ typedef struct lbm_instance {
   int64_t vstride;
   int64_t origin;
   int32_t rows;               /* interior rows: product of n over all axes but the last */
-  int32_t col_tiles;          /* tiles across the last axis: ceil(n_last / block) */
+  int32_t col_tiles;          /* tiles across the last axis: ceil(n_last / span) */
   int32_t tile_begin;         /* index of this instance's first tile */
-  int32_t reserved;
+  int32_t flags;              /* LBM_INSTANCE_* bits */
   double prm[LBM_MAX_PRM];    /* run-time parameters of this instance */
 } lbm_instance;
+
+/* A tile of this instance spans 2 x block nodes of the last axis (span =
+ * 2 block, else span = block): each thread updates two neighbouring nodes.
+ * Modules with 16-bit storage then load and store both nodes as one 32-bit
+ * word and relax them with packed FP32x2 arithmetic when n_last, origin +
+ * halo_last, vstride, the outer strides and both buffer offsets are even;
+ * otherwise the thread updates the two nodes one after the other. */
+#define LBM_INSTANCE_PAIRS 1
 
 /* One periodic step of every instance.  `arena` holds all populations (the
  * storage type of the module), `inst` (device, ninst entries) describes them
  * and `tile_instance` (device, ntiles entries) maps each tile to its
- * instance; a tile is `rows_per_tile` rows x `block` consecutive nodes of the
- * last axis.  `parity` selects which of the two buffers is read (then the
- * other is written).  `grid` blocks of `block` threads stride over the tiles
- * (grid = 0: one block per tile). */
+ * instance; a tile is `rows_per_tile` rows x `span` consecutive nodes of the
+ * last axis (span = block, or 2 x block with LBM_INSTANCE_PAIRS).  `parity`
+ * selects which of the two buffers is read (then the other is written).
+ * `grid` blocks of `block` threads stride over the tiles (grid = 0: one
+ * block per tile). */
 int lbm_ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
                       int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream);
 

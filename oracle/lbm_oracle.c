@@ -14,6 +14,8 @@
  *                        order x, y, z, full extent of the other axes, periodic)
  *   oracle_boundary      pylbm/boundary.py:430-464 / :646-680 / :787-818
  *                        (f[istore] = sign*f[iload0] + rhs, links in order)
+ *   oracle_bouzidi       pylbm/boundary.py:472-623 / :687-760 (interpolated
+ *                        bounce-back / anti-bounce-back)
  *   oracle_one_time_step pylbm/algorithm/pull.py:11-59 with
  *                        pylbm/algorithm/base.py:298-428: pull f(x - v_k),
  *                        m = M f, m_k = (1 - s_k) m_k + s_k meq_k(m_cons) for
@@ -121,6 +123,38 @@ void oracle_boundary(double* f, int dim, int nv, const int* n, const int* h, con
     if (rhs) v += rhs[c];
     f[(long long)st[0] * g.vstride + off3(&g, is[0], is[1], is[2])] = v;
   }
+}
+
+/* Bouzidi links (pylbm/boundary.py:570-618 and :707-756), in pylbm's printed
+ * order ((1 - d) f1 +/- d f0) + rhs.  anti = 0: bounce-back, whose loads read
+ * a copy of f taken before the method (pylbm/boundary.py:536-559, fcopy);
+ * anti = 1: anti-bounce-back, loads and stores in f, links in order. */
+void oracle_bouzidi(double* f, int dim, int nv, const int* n, const int* h, const int32_t* iload0,
+                    const int32_t* iload1, const int32_t* istore, int ncond, const double* rhs,
+                    const double* dist, int anti) {
+  og g = make_geo(dim, nv, 0, n, h);
+  const int w = dim + 1;
+  const double* src = f;
+  double* copy = NULL;
+  if (!anti) {
+    copy = (double*)malloc(sizeof(double) * (size_t)g.vstride * (size_t)nv);
+    memcpy(copy, f, sizeof(double) * (size_t)g.vstride * (size_t)nv);
+    src = copy;
+  }
+  for (int c = 0; c < ncond; ++c) {
+    long long o[3];
+    const int32_t* rows[3] = {iload0 + (long long)c * w, iload1 + (long long)c * w, istore + (long long)c * w};
+    for (int r = 0; r < 3; ++r) {
+      long long i[3] = {0, 0, 0};
+      for (int d = 0; d < dim; ++d) i[d] = rows[r][1 + d];
+      o[r] = (long long)rows[r][0] * g.vstride + off3(&g, i[0], i[1], i[2]);
+    }
+    const double d = dist[c];
+    const double t1 = (1 - d) * src[o[1]];
+    const double t0 = d * src[o[0]];
+    f[o[2]] = (anti ? t1 - t0 : t1 + t0) + rhs[c];
+  }
+  free(copy);
 }
 
 typedef struct {

@@ -47,12 +47,13 @@ def lib():
         P, I = ctypes.c_void_p, ctypes.c_int
         L.oracle_update_halo.argtypes = [P, I, I, P, P]
         L.oracle_boundary.argtypes = [P, I, I, P, P, P, P, I, P, ctypes.c_double]
+        L.oracle_bouzidi.argtypes = [P, I, I, P, P, P, P, P, I, P, P, I]
         L.oracle_one_time_step.argtypes = [P, P, I, I, I, P, P, P, P, P, P, I, P, P, P, I]
         L.oracle_f2m.argtypes = [P, P, I, I, P, P, P]
         L.oracle_m2f.argtypes = [P, P, I, I, P, P, P]
         L.oracle_equilibrium.argtypes = [P, I, I, I, P, P, I, P, P, P]
-        for fn in ("oracle_update_halo", "oracle_boundary", "oracle_one_time_step", "oracle_f2m", "oracle_m2f",
-                   "oracle_equilibrium"):
+        for fn in ("oracle_update_halo", "oracle_boundary", "oracle_bouzidi", "oracle_one_time_step", "oracle_f2m",
+                   "oracle_m2f", "oracle_equilibrium"):
             getattr(L, fn).restype = None
         _lib = L
     return _lib
@@ -170,14 +171,23 @@ class OracleSimulation:
         for meth in self.bc.methods:
             if meth.update_feq(self):
                 meth.set_rhs()
+            if meth.kind.startswith("bouzidi"):
+                dist = np.ascontiguousarray(meth.s, dtype=np.float64)
+                L.oracle_bouzidi(_p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h), _p(meth.iload[0]),
+                                 _p(meth.iload[1]), _p(meth.istore), meth.ncond, _p(meth.rhs), _p(dist),
+                                 1 if meth.kind == "bouzidi_anti_bounce_back" else 0)
+                continue
             sign = -1.0 if meth.kind == "anti_bounce_back" else 1.0
             rhs = meth.rhs if meth.kind != "neumann" else None
             L.oracle_boundary(_p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h), _p(meth.iload[0]),
                               _p(meth.istore), meth.ncond, _p(rhs) if rhs is not None else None, sign)
-        s, rows, coefs, expos = self._tables()
-        L.oracle_one_time_step(_p(self.f), _p(self.fnew), self.dim, sc.nv, sc.nconsm, _p(self.n), _p(self.h),
-                               _p(self.vel), _p(self.M), _p(self.invM), _p(s), len(rows), _p(rows), _p(coefs),
-                               _p(expos), self.nthreads)
+        if sc.Tu is not None or sc.source_terms:
+            self._frame_step()
+        else:
+            s, rows, coefs, expos = self._tables()
+            L.oracle_one_time_step(_p(self.f), _p(self.fnew), self.dim, sc.nv, sc.nconsm, _p(self.n), _p(self.h),
+                                   _p(self.vel), _p(self.M), _p(self.invM), _p(s), len(rows), _p(rows), _p(coefs),
+                                   _p(expos), self.nthreads)
         self.f, self.fnew = self.fnew, self.f
         self.t += self.dt
         self.nt += 1
@@ -185,6 +195,87 @@ class OracleSimulation:
     def run(self, nsteps):
         for _ in range(int(nsteps)):
             self.one_time_step()
+
+    # ---------------------------------------------------------------- relative velocity / sources
+    def _frame_functions(self):
+        """NumPy functions of the conserved moments, u and m (built once per parameter set)."""
+        from pylbm_gb300.scheme import DT
+        sc = self.scheme
+        key = tuple(sorted(self.extra_parameters_str().items()))
+        if getattr(self, "_frame_key", None) == key:
+            return self._frame
+        vals = dict(self.extra_parameters_str())
+        vals["dt"] = self.dt
+        prm = {sym: vals[str(sym)] for sym in sc.free_symbols}
+        cons = list(sc.consm.keys())
+        msym = sp.symbols(f"m0:{sc.nv}")
+        u = list(sc.rel_vel_symbols)
+        to_m = dict(zip(cons, msym[:sc.nconsm]))
+        args = list(msym) + u
+
+        def fn(exprs):
+            exprs = [sp.sympify(e).subs(prm).subs(to_m) for e in exprs]
+            return [sp.lambdify(args, e, "numpy") for e in exprs]
+
+        out = {"rel": fn(sc.rel_vel) if sc.Tu is not None else None}
+        eq = sp.Matrix(sc.EQ)
+        if sc.Tu is not None:
+            out["to_rel"] = fn([sum(sc.Tu[k, l] * msym[l] for l in range(sc.nv)) for k in range(sc.nv)])
+            out["back"] = fn([sum(sc.Tmu[k, l] * msym[l] for l in range(sc.nv)) for k in range(sc.nv)])
+            eq = sc.Tu * eq
+        out["eq"] = fn(list(eq))
+        out["src"] = [(k, f) for (k, _), f in zip(sc.source_terms,
+                                                   fn([cons[k] + DT / 2 * rhs for k, rhs in sc.source_terms]))]
+        out["s"] = sc.rates_numpy(self.extra_parameters_str())
+        self._frame, self._frame_key = out, key
+        return out
+
+    def _frame_step(self):
+        """PullAlgorithm.one_time_step_local (pylbm/algorithm/pull.py:11-59) with
+        a relative velocity (base.py f2m_local :298-334, relaxation_local
+        :404-428, restore_conserved_moments :255-263, m2f_local :346-369)
+        and/or source terms (source_term_local :439-495): conserved moments
+        M f, u = rel_vel(m), non-conserved moments T(u) M f, sources over
+        dt/2, relaxation towards T(u) m_eq, conserved moments replaced by
+        (T(u) M f)_c, sources over dt/2, f = M^-1 T(-u) m.  Float64 NumPy,
+        whole interior at once."""
+        sc = self.scheme
+        fn = self._frame_functions()
+        nv, nc, dim = sc.nv, sc.nconsm, self.dim
+        h, n = self.h, self.n
+        pulled = np.empty((nv,) + tuple(int(x) for x in n))
+        for k in range(nv):
+            sl = tuple(slice(int(h[d]) - int(self.vel[k, d]), int(h[d]) - int(self.vel[k, d]) + int(n[d]))
+                       for d in range(dim))
+            pulled[k] = self.f[(k,) + sl]
+        m = np.tensordot(self.M, pulled, axes=1)
+        zero = np.zeros_like(m[0])
+        u = [zero + f(*m, *([zero] * dim)) for f in fn["rel"]] if fn["rel"] else []
+        rel = None
+        if u:
+            rel = [zero + f(*m, *u) for f in fn["to_rel"]]
+            for k in range(nc, nv):
+                m[k] = rel[k]
+        u_args = u if u else [zero] * dim
+
+        def sources():
+            new = [(k, zero + f(*m, *u_args)) for k, f in fn["src"]]
+            for k, v in new:
+                m[k] = v
+
+        sources()
+        eq = [zero + f(*m, *u_args) for f in fn["eq"]]
+        for k in range(nv):
+            if fn["s"][k] != 0.0:
+                m[k] = m[k] + fn["s"][k] * (eq[k] - m[k])
+        if rel is not None:  # restore_conserved_moments (pylbm/algorithm/base.py:255-263, pull.py:48-49)
+            for k in range(nc):
+                m[k] = rel[k]
+        sources()
+        if u:
+            m = np.array([zero + f(*m, *u) for f in fn["back"]])
+        inner = tuple(slice(int(h[d]), int(h[d]) + int(n[d])) for d in range(dim))
+        self.fnew[(slice(None),) + inner] = np.tensordot(self.invM, m, axes=1)
 
     def moments_halo(self):
         sc = self.scheme

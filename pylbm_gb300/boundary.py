@@ -8,7 +8,8 @@ grouped per method class in the order labels, schemes, velocities are met
 (:78-160).  Each method derives its load slots (``set_iload``) and its
 right-hand side from the equilibrium at the wall points (``prepare_rhs``,
 :238-305).  The lists are uploaded once; every step the device kernels of the
-C ABI apply ``f[istore] = +/- f[iload0] + rhs``.
+C ABI apply ``f[istore] = +/- f[iload0] + rhs`` (Bouzidi methods: an
+interpolation between two loads).
 """
 from collections import OrderedDict
 
@@ -57,8 +58,8 @@ class _Moments:
 class BoundaryMethod:
     """Common part of the boundary methods (pylbm/boundary.py:164-397).
 
-    ``kind`` selects the device kernel: 'bounce_back', 'anti_bounce_back' or
-    'neumann'.
+    ``kind`` selects the device kernel: 'bounce_back', 'anti_bounce_back',
+    'bouzidi_bounce_back', 'bouzidi_anti_bounce_back' or 'neumann'.
     """
 
     kind = None
@@ -171,6 +172,66 @@ class AntiBounceBack(BounceBack):
         self.rhs[:] = self.feq[k, i] + self.feq[ksym, i]
 
 
+class BouzidiBounceBack(BoundaryMethod):
+    """Interpolated bounce-back of Bouzidi, Firdaouss and Lallemand (pylbm/boundary.py:472-623).
+
+    f_k(x_g) = (1 - s) f_l1 + s f_l0 + feq_k - feq_k', with the loads taken
+    from the populations as they were before the method ran.  For a wall at
+    distance q < 1/2 of the link: l0 = (k', x_g + v_k), l1 = (k', x_g + 2 v_k),
+    s = 2q; otherwise l0 = (k', x_g + v_k), l1 = (k, x_g + v_k), s = 1/(2q)
+    (``set_iload``, pylbm/boundary.py:508-534).
+    """
+
+    kind = "bouzidi_bounce_back"
+    name = "Bouzidi_bounce_back"
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        self.s = np.empty(self.istore.shape[1])
+
+    def set_iload(self):
+        k = self.istore[0]
+        ksym = self.stencil.get_symmetric()[k]
+        v = self.stencil.get_all_velocities()
+        iload1 = np.zeros(self.istore.shape, dtype=np.int32)
+        iload2 = np.zeros(self.istore.shape, dtype=np.int32)
+        near = self.distance < 0.5
+        far = np.logical_not(near)
+        iload1[0] = ksym
+        iload2[0, near] = ksym[near]
+        iload2[0, far] = k[far]
+        iload1[1:] = self.istore[1:] + v[k].T
+        iload2[1:, near] = self.istore[1:, near] + 2 * v[k[near]].T
+        iload2[1:, far] = self.istore[1:, far] + v[k[far]].T
+        self.s[near] = 2.0 * self.distance[near]
+        self.s[far] = 0.5 / self.distance[far]
+        self.iload.append(iload1)
+        self.iload.append(iload2)
+
+    def set_rhs(self):
+        k = self.istore[:, 0]
+        ksym = self.stencil.get_symmetric()[k]
+        i = np.arange(k.size)
+        self.rhs[:] = self.feq[k, i] - self.feq[ksym, i]
+
+
+class BouzidiAntiBounceBack(BouzidiBounceBack):
+    """Interpolated anti-bounce-back (pylbm/boundary.py:687-760).
+
+    f_k(x_g) = (1 - s) f_l1 - s f_l0 + feq_k + feq_k', loads and stores in
+    the populations themselves, links in list order.
+    """
+
+    kind = "bouzidi_anti_bounce_back"
+    name = "Bouzidi_anti_bounce_back"
+
+    def set_rhs(self):
+        k = self.istore[:, 0]
+        ksym = self.stencil.get_symmetric()[k]
+        i = np.arange(k.size)
+        self.rhs[:] = self.feq[k, i] + self.feq[ksym, i]
+
+
 class Neumann(BoundaryMethod):
     """f_k(x_g) = f_k(x_g + v_k)  (pylbm/boundary.py:763-823)."""
 
@@ -212,7 +273,8 @@ class NeumannZ(_NeumannAxis):
     axis = 2
 
 
-_BY_NAME = {c.__name__: c for c in (BounceBack, AntiBounceBack, Neumann, NeumannX, NeumannY, NeumannZ)}
+_BY_NAME = {c.__name__: c for c in (BounceBack, AntiBounceBack, BouzidiBounceBack, BouzidiAntiBounceBack,
+                                     Neumann, NeumannX, NeumannY, NeumannZ)}
 
 
 def resolve_method(cls):

@@ -58,17 +58,30 @@ class ExprPrinter:
         if e.is_Symbol:
             raise SchemeError(f"unbound symbol {e} in generated expression")
         if e.is_Add:
-            terms = [self.p(a) for a in e.args]
-            return "(" + " + ".join(terms) + ")"
-        if e.is_Mul:
-            num, den = [], []
+            # product terms after the first fold into explicit multiply-adds:
+            # c*x -> fma(c, x, acc), x*y*z -> fma(x, y*z, acc), -x*y -> fma(-x, y, acc)
+            acc = None
             for a in e.args:
-                if a.is_Pow and a.exp.is_Integer and a.exp < 0:
-                    den.append(self.p(a.base) if a.exp == -1 else self.p(sp.Pow(a.base, -a.exp)))
-                elif a.is_Rational and not a.is_Integer and a.p == 1:
-                    den.append(_lit(a.q))
+                coef, rest = a.as_coeff_Mul()
+                if acc is None:
+                    acc = self.p(a)
+                elif coef.is_Number and coef not in (1, -1) and rest != 1:
+                    acc = f"lbm_fma<R>({self.p(coef)}, {self.p(rest)}, {acc})"
+                elif rest.is_Mul and self._splittable(rest):
+                    first, tail = self._split(rest)
+                    lead = first if coef == 1 else f"(-{first})"
+                    acc = f"lbm_fma<R>({lead}, {tail}, {acc})"
+                elif rest.is_Pow and rest.exp.is_Integer and rest.exp >= 2:
+                    first = self.p(rest.base)
+                    lead = first if coef == 1 else f"(-{first})"
+                    acc = f"lbm_fma<R>({lead}, {self.p(sp.Pow(rest.base, rest.exp - 1))}, {acc})"
+                elif coef == -1:
+                    acc = f"({acc} - {self.p(rest)})"
                 else:
-                    num.append(self.p(a))
+                    acc = f"({acc} + {self.p(a)})"
+            return "(" + acc + ")"
+        if e.is_Mul:
+            num, den = self._mul_parts(e)
             s = "*".join(num) if num else "LBM_R(1)"
             if den:
                 s = f"({s})/({'*'.join(den)})"
@@ -86,6 +99,27 @@ class ExprPrinter:
                 return f"lbm_sqrt({self.p(e.base)})"
             raise SchemeError(f"unsupported power {e}")
         raise SchemeError(f"unsupported expression {e} ({type(e).__name__})")
+
+    def _mul_parts(self, e):
+        """Printed numerator and denominator factors of a product."""
+        num, den = [], []
+        for a in e.args:
+            if a.is_Pow and a.exp.is_Integer and a.exp < 0:
+                den.append(self.p(a.base) if a.exp == -1 else self.p(sp.Pow(a.base, -a.exp)))
+            elif a.is_Rational and not a.is_Integer and a.p == 1:
+                den.append(_lit(a.q))
+            else:
+                num.append(self.p(a))
+        return num, den
+
+    def _splittable(self, e):
+        num, den = self._mul_parts(e)
+        return not den and len(num) >= 2
+
+    def _split(self, e):
+        """x*y*z -> ("x", "(y*z)") for a product without divisions."""
+        num, _ = self._mul_parts(e)
+        return num[0], "(" + "*".join(num[1:]) + ")"
 
 
 def _pairs(scheme):
@@ -112,7 +146,13 @@ def _row_parity(row, pairs, selfs):
 
 
 def _emit_combo(terms):
-    """sum of coef*var, grouped by |coef|: 'c1*(x + y - z) + c2*(...)'."""
+    """sum of coef*var, grouped by |coef|.
+
+    Each group of equal |coef| is summed first; groups are then accumulated
+    with explicit multiply-adds, lbm_fma(c2, (x2 + ...), c1*(x1 + ...)), which
+    the compiler contracts for scalars and which map to the packed FP32x2 FMA
+    when two nodes are updated together.
+    """
     groups = {}
     order = []
     for c, v in terms:
@@ -125,7 +165,10 @@ def _emit_combo(terms):
         groups[key].append(("+" if c > 0 else "-", v))
     if not order:
         return "LBM_R(0)"
-    parts = []
+    if 1 in groups:  # the unit group starts the accumulator (no multiply)
+        order.remove(1)
+        order.insert(0, 1)
+    acc = None
     for key in order:
         items = groups[key]
         inner = ""
@@ -134,11 +177,11 @@ def _emit_combo(terms):
                 inner = v if sg == "+" else f"-{v}"
             else:
                 inner += f" {sg} {v}"
-        if key == 1:
-            parts.append(f"({inner})")
+        if acc is None:
+            acc = f"({inner})" if key == 1 else f"{_lit(key)}*({inner})"
         else:
-            parts.append(f"{_lit(key)}*({inner})")
-    return " + ".join(parts)
+            acc = f"lbm_fma<R>({_lit(key)}, ({inner}), {acc})"
+    return acc
 
 
 class SchemeSource:
@@ -156,17 +199,26 @@ class SchemeSource:
         "reference" (unshifted float64 only): the reference generator's
         printed expressions (refforms.ReferenceForms), compiled without fused
         multiply-adds, for parity with pylbm's generated code.
+    node_pairs : bool
+        16-bit storage, fast style: update two nodes of a row per thread with
+        packed FP32x2 arithmetic where the lattice allows it.
     """
 
-    def __init__(self, scheme, shifted, c0=None, style="fast"):
+    def __init__(self, scheme, shifted, c0=None, style="fast", node_pairs=True):
         self.scheme = scheme
+        self.node_pairs = bool(node_pairs)
         self.shifted = bool(shifted)
         if style not in ("fast", "reference"):
             raise SchemeError(f"unknown style {style!r}")
         if style == "reference" and self.shifted:
             raise SchemeError("the reference style is the unshifted float64 form")
+        if style == "reference" and (scheme.Tu is not None or scheme.source_terms):
+            raise SchemeError("the reference style covers schemes without relative velocity or source terms")
         self.style = style
-        self.nvcc_flags = ["-fmad=false"] if style == "reference" else []
+        # no implicit contraction: every fused multiply-add is an explicit
+        # lbm_fma in the generated source, so all kernels of a module (and the
+        # one- and two-node forms) round identically
+        self.nvcc_flags = ["-fmad=false"]
         self._ref = None
         nv, nc = scheme.nv, scheme.nconsm
         self.c0 = [to_fraction(c) for c in (c0 if c0 is not None else [0] * nc)]
@@ -296,8 +348,10 @@ class SchemeSource:
             eqs = pr(red[idx])
             if not isinstance(s, sp.Expr) and s == 1.0:
                 lines.append(f"{indent}{m}[{k}] = {eqs};")
+            elif red[idx] == 0:  # m + s (0 - m) = fma(-s, m, m), the same rounding
+                lines.append(f"{indent}{m}[{k}] = lbm_fma<R>(-({sstr}), {m}[{k}], {m}[{k}]);")
             else:
-                lines.append(f"{indent}{m}[{k}] = {m}[{k}] + {sstr}*({eqs} - {m}[{k}]);")
+                lines.append(f"{indent}{m}[{k}] = lbm_fma<R>({sstr}, ({eqs} - {m}[{k}]), {m}[{k}]);")
         return lines
 
     def _eq_abs_code(self, m, indent="  "):
@@ -321,6 +375,114 @@ class SchemeSource:
 
     def _relax_abs_code(self, m, indent="  "):
         return self._relax_code(m, indent, deviation=False)
+
+    # --------------------------------------------------------------- frame-relative / source-term collide
+    @property
+    def absolute_collide(self):
+        """Schemes with a relative velocity or source terms collide in absolute form."""
+        return self.scheme.Tu is not None or bool(self.scheme.source_terms)
+
+    def _names(self, m="m"):
+        sc = self.scheme
+        names = {c: f"{m}[{i}]" for i, c in enumerate(sc.consm.keys())}
+        for i, s in enumerate(self.params):
+            names[s] = f"prm[{i}]"
+        for d, u in enumerate(sc.rel_vel_symbols):
+            names[u] = f"u_{d}"
+        return names
+
+    def _assign_block(self, targets, exprs, names, prefix, indent):
+        """targets[i] = exprs[i] evaluated together (all right-hand sides first)."""
+        repl, red = sp.cse(exprs, symbols=sp.numbered_symbols(f"{prefix}c_"), optimizations="basic")
+        pr = ExprPrinter(dict(names))
+        lines = [f"{indent}{{"]
+        for sym, val in repl:
+            lines.append(f"{indent}  const R {sym} = {pr(val)};")
+            pr.names[sym] = str(sym)
+        for i, e in enumerate(red):
+            lines.append(f"{indent}  const R {prefix}{i} = {pr(e)};")
+        for i, t in enumerate(targets):
+            lines.append(f"{indent}  {t} = {prefix}{i};")
+        lines.append(f"{indent}}}")
+        return lines
+
+    def _source_code(self, names, indent):
+        """m_c += dt/2 S_c(m) for every source term (pylbm/algorithm/base.py:439-495, ode.py:11-16)."""
+        sc = self.scheme
+        if not sc.source_terms:
+            return []
+        cons = list(sc.consm.keys())
+        from .scheme import DT
+        targets, exprs = [], []
+        for k, rhs in sc.source_terms:
+            targets.append(f"m[{k}]")
+            exprs.append(cons[k] + DT / 2 * rhs)
+        return self._assign_block(targets, exprs, names, "src_", indent)
+
+    def _absolute_collide_code(self, indent="  "):
+        """One node: pull values g (stored form) -> post-collision g.
+
+        Order of pylbm's PullAlgorithm.one_time_step_local
+        (pylbm/algorithm/pull.py:11-59): moments (conserved ones absolute; the
+        others, with a relative velocity u(m_cons), seen from the frame moving
+        at u: T(u) M f), source terms over dt/2, relaxation towards
+        T(u) m_eq, the conserved moments replaced by their moving-frame values
+        (T(u) M f)_c, source terms over dt/2, and f = M^-1 T(-u) m.
+        """
+        sc = self.scheme
+        nv, nc = sc.nv, sc.nconsm
+        msym = [sp.Symbol(f"__m{l}") for l in range(nv)]
+        names = self._names()
+        lines = [f"{indent}R m[LBM_Q];"]
+        if self.shifted:
+            for k in range(nv):
+                if self.shift[k] != 0:
+                    lines.append(f"{indent}g[{k}] = g[{k}] + {_lit(self.shift[k])};")
+        lines.append(f"{indent}lbm_moments<R>(g, m);")
+        rel = sc.Tu is not None
+        if rel:
+            pr = ExprPrinter(names)
+            for d, e in enumerate(sc.rel_vel):
+                lines.append(f"{indent}const R u_{d} = {pr(e)};")
+            mnames = dict(names)
+            mnames.update({msym[l]: f"m[{l}]" for l in range(nv)})
+            # every moment in the moving frame; the conserved ones are kept
+            # aside until after the relaxation (PullAlgorithm, pull.py:48-49)
+            lines.append(f"{indent}R mc_rel[LBM_NCONS];")
+            targets = [f"mc_rel[{k}]" for k in range(nc)] + [f"m[{k}]" for k in range(nc, nv)]
+            exprs = [sp.expand(sum(sc.Tu[k, l] * msym[l] for l in range(nv))) for k in range(nv)]
+            lines += self._assign_block(targets, exprs, mnames, "rel_", indent)
+        lines += self._source_code(names, indent)
+        # relaxation of every moment with a non-zero rate towards T(u) m_eq
+        eqv = sp.Matrix(sc.EQ)
+        eq_rel = (sc.Tu * eqv).applyfunc(sp.expand) if rel else eqv
+        targets, exprs = [], []
+        for k in range(nv):
+            rate = sc.s[k]
+            if not isinstance(rate, sp.Expr) and rate == 0.0:
+                continue
+            rate = rate if isinstance(rate, sp.Expr) else sp.Float(rate)
+            targets.append(f"m[{k}]")
+            exprs.append(msym[k] + rate * (eq_rel[k] - msym[k]))
+        rnames = dict(names)
+        rnames.update({msym[l]: f"m[{l}]" for l in range(nv)})
+        if targets:
+            lines += self._assign_block(targets, exprs, rnames, "rlx_", indent)
+        if rel:  # restore_conserved_moments (pylbm/algorithm/base.py:255-263)
+            for k in range(nc):
+                lines.append(f"{indent}m[{k}] = mc_rel[{k}];")
+        lines += self._source_code(names, indent)
+        if rel:
+            targets = [f"m[{k}]" for k in range(nv)]
+            exprs = [sp.expand(sum(sc.Tmu[k, l] * msym[l] for l in range(nv))) for k in range(nv)]
+            lines += self._assign_block(targets, exprs, rnames, "back_", indent)
+        lines.append(f"{indent}lbm_populations<R>(m, g);")
+        if self.shifted:
+            for k in range(nv):
+                if self.shift[k] != 0:
+                    lines.append(f"{indent}g[{k}] = g[{k}] - {_lit(self.shift[k])};")
+        lines.append(f"{indent}(void)prm;")
+        return lines
 
     # ---------------------------------------------------------------
     def header(self):
@@ -381,10 +543,13 @@ class SchemeSource:
         out.append("}")
         out.append("template <typename R>")
         out.append("__device__ __forceinline__ void lbm_collide(R (&g)[LBM_Q], const R* __restrict__ prm) {")
-        out.append("  R m[LBM_Q];")
-        out.append("  lbm_moments<R>(g, m);")
-        out.append("  lbm_relax<R>(m, prm);")
-        out.append("  lbm_populations<R>(m, g);")
+        if self.absolute_collide:
+            out += self._absolute_collide_code()
+        else:
+            out.append("  R m[LBM_Q];")
+            out.append("  lbm_moments<R>(g, m);")
+            out.append("  lbm_relax<R>(m, prm);")
+            out.append("  lbm_populations<R>(m, g);")
         out.append("}")
         return "\n".join(out) + "\n"
 
@@ -415,11 +580,23 @@ class SchemeSource:
         return out
 
     def module_source(self, storage, compute):
-        """Full translation unit of the module for one storage/compute type."""
+        """Full translation unit of the module for one storage/compute type (memoised:
+        sympy is not thread-safe, so callers that compile in parallel generate first)."""
+        key = (storage, compute)
+        cache = self.__dict__.setdefault("_sources", {})
+        if key not in cache:
+            cache[key] = self._module_source(storage, compute)
+        return cache[key]
+
+    def _module_source(self, storage, compute):
         ctypes_ = {"float64": "double", "float32": "float", "float16": "__half", "bfloat16": "__nv_bfloat16"}
+        pairs = (self.node_pairs and self.style == "fast" and storage in ("float16", "bfloat16")
+                 and compute == "float32")
         return (f"#define LBM_STORAGE {ctypes_[storage]}\n"
                 f"#define LBM_COMPUTE {ctypes_[compute]}\n"
+                + ("#define LBM_PAIRS 1\n" if pairs else "") +
                 "#include \"lbm_common.cuh\"\n"
+                "using lbm::lbm_fma;\n"
                 "template <typename R> __device__ __forceinline__ R lbm_sqrt(R x) { return sqrt(x); }\n"
                 + self.header() +
                 "#include \"scheme_kernels.cuh\"\n")

@@ -90,6 +90,40 @@ template <> struct Store<__nv_bfloat16> {
   }
 };
 
+// ---------------------------------------------------------------- node pairs
+// Two nodes' FP32 values processed together with the packed FP32x2
+// instructions of sm_100+ (FADD2/FMUL2/FFMA2): the generated per-node algebra
+// is instantiated with this type to update two neighbouring nodes at once.
+struct F2 {
+  float2 v;
+  __device__ __forceinline__ F2() {}
+  __device__ __forceinline__ F2(float a, float b) { v = make_float2(a, b); }
+  __device__ __forceinline__ explicit F2(float a) { v = make_float2(a, a); }
+  __device__ __forceinline__ explicit F2(double a) { v = make_float2((float)a, (float)a); }
+  __device__ __forceinline__ explicit F2(int a) { v = make_float2((float)a, (float)a); }
+};
+
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { F2 r; r.v = __fadd2_rn(a.v, b.v); return r; }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { F2 r; r.v = __fmul2_rn(a.v, b.v); return r; }
+__device__ __forceinline__ F2 operator-(F2 a) { return F2(-a.v.x, -a.v.y); }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return a + (-b); }
+__device__ __forceinline__ F2 operator/(F2 a, F2 b) { return F2(a.v.x / b.v.x, a.v.y / b.v.y); }
+__device__ __forceinline__ F2& operator+=(F2& a, F2 b) { a = a + b; return a; }
+__device__ __forceinline__ F2 sqrt(F2 a) { return F2(sqrtf(a.v.x), sqrtf(a.v.y)); }
+
+// a*b + c with one rounding.  Scheme modules are compiled without implicit
+// contraction, so these are the only fused multiply-adds of the generated
+// algebra and every kernel instantiating it rounds the same way; the pair
+// form rounds each lane exactly as the scalar form.
+template <typename R>
+__device__ __forceinline__ R lbm_fma(R a, R b, R c);
+template <>
+__device__ __forceinline__ double lbm_fma<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+template <>
+__device__ __forceinline__ float lbm_fma<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <>
+__device__ __forceinline__ F2 lbm_fma<F2>(F2 a, F2 b, F2 c) { F2 r; r.v = __ffma2_rn(a.v, b.v, c.v); return r; }
+
 // ---------------------------------------------------------------- geometry
 // Kernel-side copy of lbm_lattice (without the shift table).
 struct Geo {

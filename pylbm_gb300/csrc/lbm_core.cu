@@ -99,6 +99,73 @@ __global__ void k_boundary_ordered(S* __restrict__ f, Geo g, BcArgs a) {
     for (int c = 0; c < a.ncond; ++c) bc_link(f, g, a, c);
 }
 
+// ---------------------------------------------------------------- Bouzidi
+struct BouzidiArgs {
+  const int* iload0;
+  const int* iload1;
+  const int* istore;
+  const double* rhs;
+  const double* dist;
+  double* scratch;  // copy semantics: values of every link before any store
+  int ncond;
+  int anti;         // 0: bounce-back (+d f0), 1: anti-bounce-back (-d f0)
+  double shift[LBM_MAX_Q];
+};
+
+// element offset and velocity of one (k, i0[, i1[, i2]]) row of a link list
+__device__ __forceinline__ long long link_slot(const Geo& g, const int* row, int& k) {
+  int i[3] = {0, 0, 0};
+  for (int d = 0; d < g.dim; ++d) i[d] = row[1 + d];
+  k = row[0];
+  return (long long)k * g.vstride + node_offset(g, i[0], i[1], i[2]);
+}
+
+// ((1-d) f1 +/- d f0) + rhs with separate roundings, in pylbm's printed order
+template <typename S>
+__device__ __forceinline__ double bouzidi_value(const S* f, const Geo& g, const BouzidiArgs& a, int c) {
+  const int w = g.dim + 1;
+  int k0, k1;
+  const long long o0 = link_slot(g, a.iload0 + (long long)c * w, k0);
+  const long long o1 = link_slot(g, a.iload1 + (long long)c * w, k1);
+  const double f0 = (double)Store<S>::load_plain(f + o0) + a.shift[k0];
+  const double f1 = (double)Store<S>::load_plain(f + o1) + a.shift[k1];
+  const double d = a.dist[c];
+  const double t1 = __dmul_rn(__dsub_rn(1.0, d), f1);
+  const double t0 = __dmul_rn(d, f0);
+  return __dadd_rn(a.anti ? __dsub_rn(t1, t0) : __dadd_rn(t1, t0), a.rhs[c]);
+}
+
+template <typename S>
+__device__ __forceinline__ void bouzidi_store(S* f, const Geo& g, const BouzidiArgs& a, int c, double v) {
+  int ks;
+  const long long os = link_slot(g, a.istore + (long long)c * (g.dim + 1), ks);
+  Store<S>::store(f + os, (decltype(Store<S>::load_plain(f)))(v - a.shift[ks]));
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_bouzidi(S* __restrict__ f, Geo g, BouzidiArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < a.ncond) bouzidi_store(f, g, a, c, bouzidi_value(f, g, a, c));
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_bouzidi_gather(const S* __restrict__ f, Geo g, BouzidiArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < a.ncond) a.scratch[c] = bouzidi_value(f, g, a, c);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_bouzidi_scatter(S* __restrict__ f, Geo g, BouzidiArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < a.ncond) bouzidi_store(f, g, a, c, a.scratch[c]);
+}
+
+template <typename S>
+__global__ void k_bouzidi_ordered(S* __restrict__ f, Geo g, BouzidiArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    for (int c = 0; c < a.ncond; ++c) bouzidi_store(f, g, a, c, bouzidi_value(f, g, a, c));
+}
+
 // ---------------------------------------------------------------- sums
 // Stage 1: block b of population k sums rows [b*rows_per_block, ...) of the
 // interior with FP64 warp shuffles; stage 2 adds the per-block partials.
@@ -500,6 +567,55 @@ int lbm_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, 
 int lbm_neumann(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
                 const lbm_lattice* lat, int32_t ordered, void* stream) {
   return boundary_common(f, iload0, istore, ncond, nullptr, lat, ordered, 1.0, "lbm_neumann", stream);
+}
+
+static int bouzidi_common(void* f, const int32_t* iload0, const int32_t* iload1, const int32_t* istore,
+                          int32_t ncond, const double* rhs, const double* dist, const lbm_lattice* lat,
+                          double* scratch, int anti, int ordered, const char* who, void* stream) {
+  int rc = check_lattice(lat, who);
+  if (rc) return rc;
+  if (ncond < 0) return fail(LBM_ERR_ARG, "%s: ncond=%d", who, ncond);
+  if (ncond == 0) return LBM_OK;
+  if (!f || !iload0 || !iload1 || !istore || !rhs || !dist) return fail(LBM_ERR_ARG, "%s: NULL array", who);
+  BouzidiArgs a;
+  a.iload0 = iload0;
+  a.iload1 = iload1;
+  a.istore = istore;
+  a.rhs = rhs;
+  a.dist = dist;
+  a.scratch = scratch;
+  a.ncond = ncond;
+  a.anti = anti;
+  for (int k = 0; k < LBM_MAX_Q; ++k) a.shift[k] = k < lat->nv ? lat->shift[k] : 0.0;
+  Geo g = make_geo(*lat);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int blocks = (ncond + kThreads - 1) / kThreads;
+  return dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    if (ordered) {
+      k_bouzidi_ordered<S><<<1, 1, 0, s>>>((S*)f, g, a);
+    } else if (scratch) {
+      k_bouzidi_gather<S><<<blocks, kThreads, 0, s>>>((const S*)f, g, a);
+      k_bouzidi_scatter<S><<<blocks, kThreads, 0, s>>>((S*)f, g, a);
+    } else {
+      k_bouzidi<S><<<blocks, kThreads, 0, s>>>((S*)f, g, a);
+    }
+    return launch_check(who);
+  });
+}
+
+int lbm_bouzidi_bounce_back(void* f, const int32_t* iload0, const int32_t* iload1, const int32_t* istore,
+                            int32_t ncond, const double* rhs, const double* dist, const lbm_lattice* lat,
+                            double* scratch, void* stream) {
+  return bouzidi_common(f, iload0, iload1, istore, ncond, rhs, dist, lat, scratch, 0, 0,
+                        "lbm_bouzidi_bounce_back", stream);
+}
+
+int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* iload1, const int32_t* istore,
+                                 int32_t ncond, const double* rhs, const double* dist, const lbm_lattice* lat,
+                                 int32_t ordered, void* stream) {
+  return bouzidi_common(f, iload0, iload1, istore, ncond, rhs, dist, lat, nullptr, 1, ordered,
+                        "lbm_bouzidi_anti_bounce_back", stream);
 }
 
 int lbm_restrict(const void* f, const lbm_lattice* lat, double* out, int32_t factor, void* stream) {

@@ -134,10 +134,163 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_step_periodic(const S* __restrict
   for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * a.g.vstride, g[k]);
 }
 
+// ---------------------------------------------------------------------------
+// Two nodes per thread (16-bit storage).  A thread owns nodes z and z+1 of the
+// contiguous axis (z even), loads each population of both as one 32-bit word,
+// and runs the generated algebra once on F2 = two FP32 lanes (packed FP32x2
+// instructions), halving the load/store/convert/address instructions and the
+// additions per node of the issue-bound 16-bit path.  Populations moving
+// along the contiguous axis read the neighbouring word; where the periodic
+// wrap breaks adjacency (row ends) the one wrapped value is read on its own.
+template <typename T> struct Pair;
+template <> struct Pair<__half> {
+  __device__ __forceinline__ static float2 load(const __half* p) {
+    return __half22float2(*reinterpret_cast<const __half2*>(p));
+  }
+  __device__ __forceinline__ static float one(const __half* p) { return __half2float(*p); }
+  __device__ __forceinline__ static void store(__half* p, float2 v) {
+    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(v.x, v.y);
+  }
+};
+template <> struct Pair<__nv_bfloat16> {
+  __device__ __forceinline__ static float2 load(const __nv_bfloat16* p) {
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+  }
+  __device__ __forceinline__ static float one(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+  __device__ __forceinline__ static void store(__nv_bfloat16* p, float2 v) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x, v.y);
+  }
+};
+template <> struct Pair<float> {
+  __device__ __forceinline__ static float2 load(const float* p) { return *reinterpret_cast<const float2*>(p); }
+  __device__ __forceinline__ static float one(const float* p) { return *p; }
+  __device__ __forceinline__ static void store(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+};
+
+#if defined(LBM_PAIRS) && LBM_VMAX == 1
+#define LBM_HAS_PAIRS 1
+// pulled pair of population plane `p` (already offset to node z of this row
+// and to the outer-axis neighbour), velocity component vl along the contiguous axis
+__device__ __forceinline__ lbm::F2 pull_pair(const S* __restrict__ p, int vl, int z, int nL) {
+  float lo, hi;
+  if (vl == 0) {
+    const float2 w = Pair<S>::load(p);
+    lo = w.x;
+    hi = w.y;
+  } else if (vl > 0) {  // sources z-1, z
+    const float2 w = Pair<S>::load(p);
+    hi = w.x;
+    lo = z > 0 ? Pair<S>::load(p - 2).y : Pair<S>::one(p + (nL - 1));
+  } else {  // sources z+1, z+2
+    const float2 w = Pair<S>::load(p);
+    lo = w.y;
+    hi = z + 2 < nL ? Pair<S>::load(p + 2).x : Pair<S>::one(p - z);
+  }
+  return lbm::F2(lo, hi);
+}
+
+// the velocity component along the last axis and the outer offset of population k
+#if LBM_DIM == 1
+#define LBM_VL(vx, vy, vz) (vx)
+#define LBM_OUTER(vx, vy, vz) 0LL
+#elif LBM_DIM == 2
+#define LBM_VL(vx, vy, vz) (vy)
+#define LBM_OUTER(vx, vy, vz) off0[(vx) + 1]
+#else
+#define LBM_VL(vx, vy, vz) (vz)
+#define LBM_OUTER(vx, vy, vz) (off0[(vx) + 1] + off1[(vy) + 1])
+#endif
+
+__device__ __forceinline__ void step_pair(const S* __restrict__ f, S* __restrict__ fnew, const Geo& g,
+                                          const lbm::F2 (&prm)[kPrm], int i0, int i1, int i2, int z, int nL) {
+  const long long o = lbm::node_offset(g, i0, i1, i2);
+  long long off0[3] = {0, 0, 0}, off1[3] = {0, 0, 0};
+#pragma unroll
+  for (int s = -1; s <= 1; ++s) {
+    if (LBM_DIM > 1) off0[s + 1] = wrap_off(i0, s, g.n[0], g.h[0], g.stride[0]);
+    if (LBM_DIM > 2) off1[s + 1] = wrap_off(i1, s, g.n[1], g.h[1], g.stride[1]);
+  }
+  (void)off1;
+  lbm::F2 gv[LBM_Q];
+#define LBM_PULL_PAIR(k, vx, vy, vz) \
+  gv[k] = pull_pair(f + o + (long long)(k) * g.vstride + LBM_OUTER(vx, vy, vz), LBM_VL(vx, vy, vz), z, nL);
+  LBM_FOR_EACH_V(LBM_PULL_PAIR)
+#undef LBM_PULL_PAIR
+  lbm_collide<lbm::F2>(gv, prm);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) Pair<S>::store(fnew + o + (long long)k * g.vstride, gv[k].v);
+}
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_step_periodic_pairs(const S* __restrict__ f, S* __restrict__ fnew,
+                                                                   StepArgs a) {
+  constexpr int L = LBM_DIM - 1;
+  const int z = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int nL = a.g.n[L];
+  if (z >= nL) return;
+  int i0, i1, i2;
+#if LBM_DIM == 1
+  i0 = z + a.g.h[0];
+  i1 = i2 = 0;
+#elif LBM_DIM == 2
+  i0 = blockIdx.y + a.g.h[0];
+  i1 = z + a.g.h[1];
+  i2 = 0;
+#else
+  i0 = blockIdx.z + a.g.h[0];
+  i1 = blockIdx.y + a.g.h[1];
+  i2 = z + a.g.h[2];
+#endif
+  lbm::F2 prm[kPrm];
+#pragma unroll
+  for (int p = 0; p < kPrm; ++p) prm[p] = lbm::F2((float)a.prm[p]);
+  step_pair(f, fnew, a.g, prm, i0, i1, i2, z, nL);
+}
+#else
+#define LBM_HAS_PAIRS 0
+#endif
+
+// halo coordinates of interior row r (all axes but the last) and column col
+__device__ __forceinline__ void row_coords(const Geo& g, int r, int col, int (&idx)[3]) {
+  constexpr int L = LBM_DIM - 1;
+  idx[0] = idx[1] = idx[2] = 0;
+  int q = r;
+#pragma unroll
+  for (int d = L - 1; d >= 0; --d) {
+    idx[d] = q % g.n[d] + g.h[d];
+    q /= g.n[d];
+  }
+  idx[L] = col + g.h[L];
+}
+
+__device__ __forceinline__ void step_node(const S* __restrict__ f, S* __restrict__ fnew, const Geo& g,
+                                          const R (&prm)[kPrm], int i0, int i1, int i2) {
+  const long long o = lbm::node_offset(g, i0, i1, i2);
+  long long off0[2 * LBM_VMAX + 1], off1[2 * LBM_VMAX + 1], off2[2 * LBM_VMAX + 1];
+#pragma unroll
+  for (int s = -LBM_VMAX; s <= LBM_VMAX; ++s) {
+    off0[s + LBM_VMAX] = LBM_DIM > 0 ? wrap_off(i0, s, g.n[0], g.h[0], g.stride[0]) : 0;
+    off1[s + LBM_VMAX] = LBM_DIM > 1 ? wrap_off(i1, s, g.n[1], g.h[1], g.stride[1]) : 0;
+    off2[s + LBM_VMAX] = LBM_DIM > 2 ? wrap_off(i2, s, g.n[2], g.h[2], g.stride[2]) : 0;
+  }
+  R gv[LBM_Q];
+#define LBM_PULL_ENS(k, vx, vy, vz)                                                              \
+  gv[k] = (R)Store<S>::load(f + o + (long long)(k) * g.vstride + off0[(vx) + LBM_VMAX] +        \
+                            off1[(vy) + LBM_VMAX] + off2[(vz) + LBM_VMAX]);
+  LBM_FOR_EACH_V(LBM_PULL_ENS)
+#undef LBM_PULL_ENS
+  R p[kPrm];
+#pragma unroll
+  for (int i = 0; i < kPrm; ++i) p[i] = prm[i];
+  lbm_collide<R>(gv, p);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * g.vstride, gv[k]);
+}
+
 // Ensemble step: blocks stride over a tile list that covers every instance;
-// a tile is rows_per_tile rows x blockDim.x nodes of the last axis of one
-// instance.  The per-node work is the periodic step above with the
-// instance's own geometry and run-time parameters.
+// a tile is rows_per_tile rows x span nodes of the last axis of one instance
+// (span = blockDim.x, or 2 blockDim.x for LBM_INSTANCE_PAIRS, where a thread
+// updates two neighbouring nodes).  The per-node work is the periodic step
+// above with the instance's own geometry and run-time parameters.
 __global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, const lbm_instance* __restrict__ inst,
                                                          const int* __restrict__ tile_inst, int ntiles,
                                                          int rows_per_tile, int parity) {
@@ -147,9 +300,9 @@ __global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, c
     const int local = tile - I->tile_begin;
     const int rt = local / I->col_tiles;
     const int ct = local - rt * I->col_tiles;
-    const int col = ct * blockDim.x + threadIdx.x;
+    const bool two = (I->flags & LBM_INSTANCE_PAIRS) != 0;
+    const int base = ct * (two ? 2 * (int)blockDim.x : (int)blockDim.x);
     const int nL = I->n[L];
-    if (col >= nL) continue;
     Geo g;
     g.dim = LBM_DIM;
     g.nv = LBM_Q;
@@ -160,40 +313,40 @@ __global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, c
     }
     g.vstride = I->vstride;
     g.origin = I->origin;
-    R prm[kPrm];
-#pragma unroll
-    for (int p = 0; p < kPrm; ++p) prm[p] = (R)I->prm[p < LBM_MAX_PRM ? p : 0];
     const S* __restrict__ f = arena + I->offset[parity];
     S* __restrict__ fnew = arena + I->offset[parity ^ 1];
     const int r0 = rt * rows_per_tile;
     const int r1 = min(I->rows, r0 + rows_per_tile);
-    for (int r = r0; r < r1; ++r) {
-      int idx[3] = {0, 0, 0};
-      int q = r;
+#if LBM_HAS_PAIRS
+    bool aligned = two && nL % 2 == 0 && (g.origin + g.h[L]) % 2 == 0 && g.vstride % 2 == 0 &&
+                   I->offset[0] % 2 == 0 && I->offset[1] % 2 == 0;
 #pragma unroll
-      for (int d = L - 1; d >= 0; --d) {
-        idx[d] = q % g.n[d] + g.h[d];
-        q /= g.n[d];
+    for (int d = 0; d < L; ++d) aligned = aligned && g.stride[d] % 2 == 0;
+    if (aligned) {
+      const int z = base + 2 * (int)threadIdx.x;
+      if (z >= nL) continue;
+      lbm::F2 prm2[kPrm];
+#pragma unroll
+      for (int p = 0; p < kPrm; ++p) prm2[p] = lbm::F2((float)I->prm[p < LBM_MAX_PRM ? p : 0]);
+      for (int r = r0; r < r1; ++r) {
+        int idx[3];
+        row_coords(g, r, z, idx);
+        step_pair(f, fnew, g, prm2, idx[0], idx[1], idx[2], z, nL);
       }
-      idx[L] = col + g.h[L];
-      const int i0 = idx[0], i1 = idx[1], i2 = idx[2];
-      const long long o = lbm::node_offset(g, i0, i1, i2);
-      long long off0[2 * LBM_VMAX + 1], off1[2 * LBM_VMAX + 1], off2[2 * LBM_VMAX + 1];
+      continue;
+    }
+#endif
+    R prm[kPrm];
 #pragma unroll
-      for (int s = -LBM_VMAX; s <= LBM_VMAX; ++s) {
-        off0[s + LBM_VMAX] = LBM_DIM > 0 ? wrap_off(i0, s, g.n[0], g.h[0], g.stride[0]) : 0;
-        off1[s + LBM_VMAX] = LBM_DIM > 1 ? wrap_off(i1, s, g.n[1], g.h[1], g.stride[1]) : 0;
-        off2[s + LBM_VMAX] = LBM_DIM > 2 ? wrap_off(i2, s, g.n[2], g.h[2], g.stride[2]) : 0;
+    for (int p = 0; p < kPrm; ++p) prm[p] = (R)I->prm[p < LBM_MAX_PRM ? p : 0];
+    for (int c = 0; c < (two ? 2 : 1); ++c) {
+      const int col = base + (int)threadIdx.x + c * (int)blockDim.x;
+      if (col >= nL) break;
+      for (int r = r0; r < r1; ++r) {
+        int idx[3];
+        row_coords(g, r, col, idx);
+        step_node(f, fnew, g, prm, idx[0], idx[1], idx[2]);
       }
-      R gv[LBM_Q];
-#define LBM_PULL_ENS(k, vx, vy, vz)                                                              \
-  gv[k] = (R)Store<S>::load(f + o + (long long)(k) * g.vstride + off0[(vx) + LBM_VMAX] +        \
-                            off1[(vy) + LBM_VMAX] + off2[(vz) + LBM_VMAX]);
-      LBM_FOR_EACH_V(LBM_PULL_ENS)
-#undef LBM_PULL_ENS
-      lbm_collide<R>(gv, prm);
-#pragma unroll
-      for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * g.vstride, gv[k]);
     }
   }
 }
@@ -421,6 +574,16 @@ inline dim3 node_grid(const lbm_lattice& l, bool with_halo) {
   return dim3(gx, gy, gz);
 }
 
+// Two-node words need an even row length and every pair (z, z+1), z even, on a
+// 4-byte boundary: even element offsets of the row start, strides and planes.
+inline bool pairs_fit(const lbm_lattice& l, const void* f, const void* fnew) {
+  const int L = LBM_DIM - 1;
+  if (l.n[L] % 2 || (l.origin + l.halo[L]) % 2 || l.vstride % 2) return false;
+  for (int d = 0; d < L; ++d)
+    if (l.stride[d] % 2) return false;
+  return ((uintptr_t)f % 4 == 0) && ((uintptr_t)fnew % 4 == 0);
+}
+
 inline StepArgs make_step_args(const lbm_lattice& l, const double* prm) {
   StepArgs a;
   a.g = lbm::make_geo(l);
@@ -463,6 +626,13 @@ static int step_common(const void* f, void* fnew, const lbm_lattice* lat, const 
   StepArgs a = make_step_args(*lat, prm);
   dim3 grid = node_grid(*lat, false);
   cudaStream_t s = (cudaStream_t)stream;
+#if LBM_HAS_PAIRS
+  if (periodic && pairs_fit(*lat, f, fnew)) {
+    grid.x = (unsigned)((lat->n[LBM_DIM - 1] / 2 + LBM_BLOCK - 1) / LBM_BLOCK);
+    k_step_periodic_pairs<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a);
+    return lbm::launch_check(who);
+  }
+#endif
   if (periodic)
     k_step_periodic<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a);
   else

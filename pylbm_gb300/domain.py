@@ -120,7 +120,7 @@ class Domain:
                     continue
                 for row, d in rows:
                     sl = [slice(None)] * self.dim
-                    sl[axis] = row
+                    sl[axis] = slice(row, row + 1 if row != -1 else None)  # a view, also in 1D
                     dv = dist[k][tuple(sl)]
                     fv = flag[k][tuple(sl)]
                     upd = dv > d

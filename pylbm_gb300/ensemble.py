@@ -50,9 +50,12 @@ class Ensemble:
         storage type ("float32", "float16", "bfloat16" shifted; "float64").
     tile : (block, rows_per_tile, grid) or None
         fixed tile shape; None runs the autotuner.
+    pairs : bool or None
+        threads update two neighbouring nodes (lbm_gb300.h,
+        LBM_INSTANCE_PAIRS); default: on for 16-bit storage.
     """
 
-    def __init__(self, dicos, params=None, dtype="float16", tile=None, c0=None):
+    def __init__(self, dicos, params=None, dtype="float16", tile=None, c0=None, pairs=None):
         if not dicos:
             raise ValueError("an ensemble needs at least one instance")
         params = params or [{} for _ in dicos]
@@ -61,19 +64,21 @@ class Ensemble:
         self.storage = dtype
         self.compute = "float64" if dtype == "float64" else "float32"
         self.shifted = dtype != "float64"
+        self.pairs = (dtype in ("float16", "bfloat16")) if pairs is None else bool(pairs)
         self.scheme = Scheme(dicos[0])
         self.dicos = dicos
         self.params = [{str(k): float(v) for k, v in p.items()} for p in params]
         names = [str(s) for s in self.scheme.free_symbols]
         if len(names) > runtime.LBM_MAX_PRM:
             raise ValueError("too many run-time parameters for an ensemble")
-        for p in self.params:
-            missing = [n for n in names if n not in p]
+        self.domains = []
+        for i, d in enumerate(dicos):
+            dom = Domain(d, self.scheme.stencil, with_flags=False)
+            # time step of the source-term integrator: the instance's dx / la
+            self.params[i].setdefault("dt", dom.dx / self.scheme.la_float)
+            missing = [n for n in names if n not in self.params[i]]
             if missing:
                 raise ValueError(f"missing run-time parameters {missing}")
-        self.domains = []
-        for d in dicos:
-            dom = Domain(d, self.scheme.stencil, with_flags=False)
             if dom.dim != self.scheme.dim:
                 raise ValueError("dimension mismatch between instances")
             self.domains.append(dom)
@@ -143,7 +148,11 @@ class Ensemble:
             I.vstride = lat.vstride
             I.origin = lat.origin
             I.rows = int(np.prod([lat.n[d] for d in range(L)])) if L > 0 else 1
-            I.col_tiles = -(-lat.n[L] // block)
+            even = [lat.n[L], lat.origin + lat.halo[L], lat.vstride, *self.offsets[i]]
+            even += [lat.stride[d] for d in range(L)]
+            I.flags = runtime.LBM_INSTANCE_PAIRS if self.pairs and all(x % 2 == 0 for x in even) else 0
+            span = 2 * block if I.flags else block
+            I.col_tiles = -(-lat.n[L] // span)
             row_tiles = -(-I.rows // rows)
             I.tile_begin = len(tile_map)
             tile_map.extend([i] * (row_tiles * I.col_tiles))
@@ -297,7 +306,7 @@ def _cache_path():
 def _signature(ens):
     sm, name = runtime.device_info()
     sizes = sorted(tuple(lat.n[d] for d in range(3)) for lat in ens.lats)
-    text = json.dumps([name, sm, ens.module.key, ens.storage, sizes])
+    text = json.dumps([name, sm, ens.module.key, ens.storage, ens.pairs, sizes])
     return hashlib.sha256(text.encode()).hexdigest()[:20], sm
 
 

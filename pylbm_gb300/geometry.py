@@ -3,7 +3,8 @@
 The reference describes obstacles by elements with ``get_bounds``,
 ``point_inside`` and a ray distance ``distance(grid, v, dmax)`` returning the
 fraction of the lattice link before the wall and the wall label
-(pylbm/elements/circle.py:24, pylbm/elements/utils.py:93 ``distance_ellipse``).
+(pylbm/elements/circle.py:24, pylbm/elements/utils.py:93 ``distance_ellipse``;
+pylbm/elements/parallelogram.py:21 with utils.py:40 ``distance_lines``).
 Boundary link lists are derived from those distances, so the ray/obstacle
 intersection follows the same quadratic (same coefficients, same smallest
 positive root, links whose root lies in (0, dmax]) to give identical lists.
@@ -79,3 +80,66 @@ class Circle(Element):
         x, y = grid
         r = self.radius
         return _ellipse_ray(x, y, v, self.center, r * np.array([1, 0]), r * np.array([0, 1]), dmax, self.label)
+
+
+def _line_hits(px, py, v, q, w):
+    """Ray (px, py) + t v against the segment q + s w, s in [0, 1]: (t, s) by
+    Cramer's rule, or None for parallel lines."""
+    det = v[1] * w[0] - v[0] * w[1]
+    if det == 0:
+        return None
+    inv = 1.0 / det
+    c1 = q[0] - px
+    c2 = q[1] - py
+    return (-w[1] * c1 + w[0] * c2) * inv, (-v[1] * c1 + v[0] * c2) * inv
+
+
+class Parallelogram(Element):
+    """Parallelogram {point + a v1 + b v2, a, b in [0, 1]} (pylbm/elements/parallelogram.py:21).
+
+    Four edges, each with its own label (edges from the point along v1 and
+    v2, then the opposite ones); the edges count as inside.
+    """
+
+    number_of_bounds = 4
+
+    def __init__(self, point, vecta, vectb, label=0, isfluid=False):
+        self.dim = 2
+        self.point = np.asarray(point, dtype=np.float64)
+        self.v1 = np.asarray(vecta, dtype=np.float64)
+        self.v2 = np.asarray(vectb, dtype=np.float64)
+        super().__init__(label, isfluid)
+
+    def get_bounds(self):
+        box = np.asarray([self.point, self.point + self.v1, self.point + self.v1 + self.v2, self.point + self.v2])
+        return np.min(box, axis=0), np.max(box, axis=0)
+
+    def point_inside(self, grid):
+        x, y = grid
+        dx, dy = x - self.point[0], y - self.point[1]
+        inv = 1.0 / (self.v1[0] * self.v2[1] - self.v1[1] * self.v2[0])
+        a = (dx * self.v2[1] - dy * self.v2[0]) * inv
+        b = (dy * self.v1[0] - dx * self.v1[1]) * inv
+        return (a >= 0) & (b >= 0) & (a <= 1) & (b <= 1)
+
+    def distance(self, grid, v, dmax=None):
+        x, y = grid
+        px, py = x - self.point[0], y - self.point[1]
+        shape = (x.size, y.size) if x.shape[1] == 1 and y.shape[0] == 1 else x.shape
+        alpha = np.full(shape, _FAR)
+        border = -np.ones(shape)
+        zero = np.zeros(2)
+        for q, w, lab in ((zero, self.v1, self.label[0]), (zero, self.v2, self.label[1]),
+                          (self.v2, self.v1, self.label[2]), (self.v1, self.v2, self.label[3])):
+            hit = _line_hits(px, py, v, q, w)
+            if hit is None:
+                continue
+            t, s = hit
+            ok = (t > 0) & (s >= 0) & (s <= 1)
+            if dmax is not None:
+                ok &= t <= dmax
+            closer = np.where(ok & (alpha > t))
+            alpha[closer] = t[closer]
+            border[closer] = lab
+        alpha[alpha == _FAR] = -1.0
+        return alpha, border

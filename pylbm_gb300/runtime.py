@@ -57,6 +57,7 @@ class Lattice(ctypes.Structure):
 
 
 LBM_MAX_PRM = 8
+LBM_INSTANCE_PAIRS = 1
 
 
 class Instance(ctypes.Structure):
@@ -72,7 +73,7 @@ class Instance(ctypes.Structure):
         ("rows", ctypes.c_int32),
         ("col_tiles", ctypes.c_int32),
         ("tile_begin", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
         ("prm", ctypes.c_double * LBM_MAX_PRM),
     ]
 
@@ -169,6 +170,8 @@ def core():
             _sig(lib, "lbm_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_anti_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_neumann", I32, [P, P, P, I32, LP, I32, P])
+            _sig(lib, "lbm_bouzidi_bounce_back", I32, [P, P, P, P, I32, P, P, LP, P, P])
+            _sig(lib, "lbm_bouzidi_anti_bounce_back", I32, [P, P, P, P, I32, P, P, LP, I32, P])
             _sig(lib, "lbm_population_sums_scratch_bytes", I32, [LP, ctypes.POINTER(SZ)])
             _sig(lib, "lbm_population_sums", I32, [P, LP, P, P, P, SZ, P])
             _sig(lib, "lbm_population_sums_noalloc", I32, [P, LP, P, P, P])

@@ -30,6 +30,12 @@ class SchemeError(ValueError):
     """Raised for scheme dictionaries the CUDA backend does not handle."""
 
 
+# velocity of the moving frame (pylbm/symbolic.py rel_ux, rel_uy, rel_uz) and
+# the time step of the source-term integrator (pylbm/algorithm/ode.py:15)
+REL_U = sp.symbols("rel_ux, rel_uy, rel_uz")
+DT = sp.Symbol("dt")
+
+
 def _box_dim(dico):
     if "dim" in dico and dico["dim"]:
         return int(dico["dim"])
@@ -100,8 +106,6 @@ class Scheme:
     """
 
     def __init__(self, dico):
-        if dico.get("relative_velocity") is not None:
-            raise SchemeError("relative_velocity schemes are not supported by the CUDA backend")
         self.dico = dico
         self.dim = _box_dim(dico)
         schemes = dico["schemes"]
@@ -114,8 +118,6 @@ class Scheme:
         self.la = to_fraction(la_val)
         self.la_float = float(self.la)
         for s in schemes:
-            if "source_terms" in s and s["source_terms"]:
-                raise SchemeError("source terms are not supported by the CUDA backend")
             if "feq" in s and s["feq"]:
                 raise SchemeError("'feq' equilibria are not supported; give 'equilibrium'")
             if "M" in s:
@@ -128,6 +130,10 @@ class Scheme:
         nv = self.nv
         mfrac = [[Fraction(0)] * nv for _ in range(nv)]
         polys = []
+        self.rel_vel_symbols = list(REL_U[:self.dim])
+        rel_vel = dico.get("relative_velocity")
+        mu_rows = [[sp.Integer(0)] * nv for _ in range(nv)] if rel_vel is not None else None
+        la_sym = sp.Rational(self.la.numerator, self.la.denominator)
         for isch, s in enumerate(schemes):
             v = [self._vel(n) for n in self.stencil.num(isch)]
             base = int(self.stencil.nv_ptr[isch])
@@ -144,6 +150,12 @@ class Scheme:
                     subs_named = [(str(coords[d]), subs[coords[d]]) for d in range(self.dim)]
                     val = p.subs(subs_named)
                     mfrac[base + i][base + j] = to_fraction(sp.nsimplify(val, rational=True))
+                    if mu_rows is not None:
+                        # moments of the populations seen from a frame moving at u
+                        # (pylbm/scheme.py:494-500): P_i(v_j la - u)
+                        pr = sp.nsimplify(p, rational=True)
+                        shifted = [(str(coords[d]), sp.Rational(vj[d]) * la_sym - REL_U[d]) for d in range(self.dim)]
+                        mu_rows[base + i][base + j] = sp.expand(pr.subs(shifted))
         self.polynomials = polys
 
         eq = []
@@ -179,6 +191,8 @@ class Scheme:
             eq[ic], eq[c] = eq[c], eq[ic]
             rates[ic], rates[c] = rates[c], rates[ic]
             mfrac[ic], mfrac[c] = mfrac[c], mfrac[ic]
+            if mu_rows is not None:
+                mu_rows[ic], mu_rows[c] = mu_rows[c], mu_rows[ic]
         for ic, c in enumerate(list(consm.keys())):
             consm[c] = ic
         self.consm = consm
@@ -189,9 +203,38 @@ class Scheme:
         self.invM_frac = exact_inverse(mfrac)
         self.M = np.array([[float(x) for x in row] for row in mfrac])
         self.invM = np.array([[float(x) for x in row] for row in self.invM_frac])
+        psubs = list(self.param.items())
+
+        # relative velocity (pylbm/scheme.py:149, :494-532): T(u) maps the
+        # moments M f to the moments P_i(v la - u) f of a frame moving at u;
+        # with M and M^-1 already permuted, T(u) = M_u M^-1 is permuted alike
+        self.Tu = self.Tmu = self.rel_vel = None
+        if mu_rows is not None:
+            inv = sp.Matrix([[sp.Rational(x.numerator, x.denominator) for x in row] for row in self.invM_frac])
+            tu = (sp.Matrix(mu_rows) * inv).applyfunc(sp.expand)
+            self.Tu = tu
+            self.Tmu = tu.subs(list(zip(REL_U, [-u for u in REL_U])), simultaneous=True).applyfunc(sp.expand)
+            if len(rel_vel) != self.dim:
+                raise SchemeError("relative_velocity needs one expression per space dimension")
+            self.rel_vel = [sp.nsimplify(sp.sympify(e).subs(psubs), rational=True) for e in rel_vel]
+
+        # source terms (pylbm/algorithm/base.py:141-150, :439-495): conserved
+        # moment -> right-hand side, integrated by explicit Euler over dt/2
+        # before and after the relaxation
+        self.source_terms = []
+        for isch, s in enumerate(schemes):
+            for key, val in (s.get("source_terms") or {}).items():
+                key = sp.Symbol(key) if isinstance(key, str) else key
+                if key not in consm:
+                    raise SchemeError(f"source term on {key}, which is not a conserved moment")
+                rhs = sp.sympify(val).subs(psubs)
+                rhs = rhs if rhs.free_symbols else sp.nsimplify(rhs, rational=True)
+                bad = rhs.free_symbols & ({c for c in coords if isinstance(c, sp.Symbol)} | {sp.Symbol("t")})
+                if bad:
+                    raise SchemeError(f"source terms depending on {sorted(map(str, bad))} are not supported")
+                self.source_terms.append((consm[key], rhs))
 
         # equilibrium and rates with parameters substituted
-        psubs = list(self.param.items())
         self.EQ = [sp.nsimplify(sp.sympify(e).subs(psubs)) if sp.sympify(e).subs(psubs).free_symbols
                    else sp.nsimplify(sp.sympify(e).subs(psubs), rational=True) for e in eq]
         self.s = []
@@ -208,6 +251,12 @@ class Scheme:
         for r in self.s:
             if isinstance(r, sp.Expr):
                 free |= r.free_symbols
+        for e in (self.rel_vel or []):
+            free |= e.free_symbols
+        for _, e in self.source_terms:
+            free |= e.free_symbols
+        if self.source_terms:
+            free.add(DT)
         coord_syms = {c for c in coords if isinstance(c, sp.Symbol)}
         if free & coord_syms:
             raise SchemeError("space-dependent equilibria are not supported by the CUDA backend")
@@ -227,7 +276,14 @@ class Scheme:
         cons = np.asarray(cons, dtype=np.float64)
         n = cons.shape[1]
         syms = list(self.consm.keys()) + list(self.free_symbols)
-        vals = [cons[i] for i in range(self.nconsm)] + [np.full(n, float(params[str(s)] if str(s) in params else params[s])) for s in self.free_symbols]
+        needed = set().union(*(e.free_symbols for e in self.EQ))
+
+        def value(s):
+            if s not in needed:  # e.g. the time step of source terms: not in the equilibrium
+                return np.zeros(n)
+            return np.full(n, float(params[str(s)] if str(s) in params else params[s]))
+
+        vals = [cons[i] for i in range(self.nconsm)] + [value(s) for s in self.free_symbols]
         out = np.empty((self.nv, n))
         for k, e in enumerate(self.EQ):
             f = sp.lambdify(syms, e, "numpy")

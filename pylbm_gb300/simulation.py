@@ -104,16 +104,25 @@ class Simulation:
         float64 only: evaluate the per-node algebra in the reference
         generator's printed form (refforms), compiled without FMA, so results
         track pylbm's Cython code; False uses the faster exact-constant form.
+    node_pairs : bool
+        16-bit storage on periodic domains: one thread updates two
+        neighbouring nodes with packed FP32x2 arithmetic (bit-identical to
+        one node per thread, fewer instructions per node).
+    c0 : sequence of float or None
+        reference state of the conserved moments for shifted storage
+        (default: the mean of the initial fields, 4 significant digits).
     """
 
     def __init__(self, dico, sorder=None, dtype="float64", check_inverse=False, initialize=True,
-                 shifted=None, parity=True):
+                 shifted=None, parity=True, node_pairs=True, c0=None):
         gen = str(dico.get("generator", "cuda")).upper()
         if gen != "CUDA":
             raise ValueError(f"pylbm_gb300 implements generator='cuda', not {gen!r}")
         if dtype not in _STORAGES:
             raise ValueError(f"dtype must be one of {_STORAGES}")
         self.parity = bool(parity)
+        self.node_pairs = bool(node_pairs)
+        self.c0 = None if c0 is None else [float(c) for c in c0]
         self.dico = dico
         self.scheme = Scheme(dico)
         lab = dico["box"].get("label", -1)
@@ -176,7 +185,8 @@ class Simulation:
         symbols that appear there (as pylbm, which takes ``extra_parameters``
         after construction); a step needs them all.
         """
-        vals = self.extra_parameters_str()
+        vals = dict(self.extra_parameters_str())
+        vals.setdefault("dt", self.dt)  # time step of the source-term integrator
         names = [str(s) for s in self.scheme.free_symbols]
         needed = set(names)
         if for_init:
@@ -239,9 +249,14 @@ class Simulation:
         if self.init_type == "distributions":
             arr = np.einsum("ij,j...->i...", sc.M, arr)
         inner = tuple(slice(int(h), -int(h)) for h in self.domain.halo)
-        c0 = [_round_reference(arr[c][inner]) for c in range(sc.nconsm)] if self.shifted else None
-        style = "reference" if (self.storage == "float64" and not self.shifted and self.parity) else "fast"
-        src = SchemeSource(sc, self.shifted, c0, style=style)
+        c0 = None
+        if self.shifted:
+            c0 = self.c0 if self.c0 is not None else [_round_reference(arr[c][inner]) for c in range(sc.nconsm)]
+        # the printed-form parity style covers the plain MRT step; schemes with a
+        # relative velocity or source terms use the exact-constant form
+        plain = sc.Tu is None and not sc.source_terms
+        style = "reference" if (self.storage == "float64" and not self.shifted and self.parity and plain) else "fast"
+        src = SchemeSource(sc, self.shifted, c0, style=style, node_pairs=self.node_pairs)
         self.module = runtime.SchemeModule(src, self.storage, self.compute)
         for k in range(nv):
             self._lat.shift[k] = float(self.module.shift[k])
@@ -270,38 +285,59 @@ class Simulation:
         self._drop_graph()
         self._need_init = False
 
+    def _device_array(self, a, itemsize):
+        buf = runtime.DeviceBuffer(max(a.nbytes, itemsize))
+        buf.upload(a, stream=self._stream)
+        return buf
+
+    def _check_links(self, meth):
+        """Every slot of the method's lists lies in the halo box (no device-side check)."""
+        hi = np.array([self.scheme.nv] + [n + 2 * int(h) for n, h in zip(self.domain.shape_in, self.domain.halo)])
+        for lst in [meth.istore] + list(meth.iload):
+            if lst.size and (lst.min() < 0 or np.any(lst.max(axis=0) >= hi)):
+                raise ValueError(f"{type(meth).__name__}: link list outside the lattice")
+
     def _upload_bc(self):
         self._bc_dev = []
         for meth in self.bc.methods:
-            il = runtime.DeviceBuffer(max(meth.iload[0].nbytes, 4))
-            il.upload(meth.iload[0], stream=self._stream)
-            st = runtime.DeviceBuffer(max(meth.istore.nbytes, 4))
-            st.upload(meth.istore, stream=self._stream)
-            rhs = runtime.DeviceBuffer(max(meth.rhs.nbytes, 8))
-            rhs.upload(meth.rhs, stream=self._stream)
-            ordered = 0 if self._links_independent(meth) else 1
-            self._bc_dev.append((meth, il, st, rhs, ordered))
+            self._check_links(meth)
+            dev = {"iload": [self._device_array(il, 4) for il in meth.iload],
+                   "istore": self._device_array(meth.istore, 4),
+                   "rhs": self._device_array(meth.rhs, 8),
+                   "ordered": 0 if self._links_independent(meth) else 1}
+            if meth.kind.startswith("bouzidi"):
+                dev["dist"] = self._device_array(np.ascontiguousarray(meth.s, dtype=np.float64), 8)
+                # copy semantics of the bounce-back: compute every link before storing
+                dev["scratch"] = runtime.DeviceBuffer(8 * max(meth.ncond, 1)) if dev["ordered"] else None
+            self._bc_dev.append((meth, dev))
 
     @staticmethod
     def _links_independent(meth):
         """True when no link reads a slot another link of the method writes."""
         st = {tuple(r) for r in meth.istore.tolist()}
-        return not any(tuple(r) in st for r in meth.iload[0].tolist())
+        return not any(tuple(r) in st for il in meth.iload for r in il.tolist())
 
     # ------------------------------------------------------------------ step
     def _enqueue_boundary(self, F):
         lat = ctypes.byref(self._lat)
         runtime.check(self._core.lbm_update_halo(F.handle, lat, self._stream))
-        for meth, il, st, rhs, ordered in self._bc_dev:
+        for meth, dev in self._bc_dev:
+            il, st, rhs, ordered = dev["iload"], dev["istore"].handle, dev["rhs"].handle, dev["ordered"]
             if meth.kind == "bounce_back":
-                rc = self._core.lbm_bounce_back(F.handle, il.handle, st.handle, meth.ncond, rhs.handle, lat,
-                                                ordered, self._stream)
+                rc = self._core.lbm_bounce_back(F.handle, il[0].handle, st, meth.ncond, rhs, lat, ordered,
+                                                self._stream)
             elif meth.kind == "anti_bounce_back":
-                rc = self._core.lbm_anti_bounce_back(F.handle, il.handle, st.handle, meth.ncond, rhs.handle,
-                                                     lat, ordered, self._stream)
+                rc = self._core.lbm_anti_bounce_back(F.handle, il[0].handle, st, meth.ncond, rhs, lat, ordered,
+                                                     self._stream)
+            elif meth.kind == "bouzidi_bounce_back":
+                scratch = dev["scratch"].handle if dev["scratch"] is not None else None
+                rc = self._core.lbm_bouzidi_bounce_back(F.handle, il[0].handle, il[1].handle, st, meth.ncond, rhs,
+                                                        dev["dist"].handle, lat, scratch, self._stream)
+            elif meth.kind == "bouzidi_anti_bounce_back":
+                rc = self._core.lbm_bouzidi_anti_bounce_back(F.handle, il[0].handle, il[1].handle, st, meth.ncond,
+                                                             rhs, dev["dist"].handle, lat, ordered, self._stream)
             else:
-                rc = self._core.lbm_neumann(F.handle, il.handle, st.handle, meth.ncond, lat, ordered,
-                                            self._stream)
+                rc = self._core.lbm_neumann(F.handle, il[0].handle, st, meth.ncond, lat, ordered, self._stream)
             runtime.check(rc)
 
     def set_closure(self, model):
@@ -311,6 +347,8 @@ class Simulation:
         """
         if model is not None and not self.periodic:
             raise ValueError("the learned closure runs on periodic domains")
+        if model is not None and (self.scheme.Tu is not None or self.scheme.source_terms):
+            raise ValueError("the learned closure corrects the plain MRT relaxation only")
         self.closure = model
         self._drop_graph()
 
@@ -334,10 +372,10 @@ class Simulation:
         """Ghost refresh then every boundary method (pylbm/simulation.py:374-390)."""
         if self.periodic:
             return
-        for meth, il, st, rhs, ordered in self._bc_dev:
+        for meth, dev in self._bc_dev:
             if meth.update_feq(self):
                 meth.set_rhs()
-                rhs.upload(meth.rhs, stream=self._stream)
+                dev["rhs"].upload(meth.rhs, stream=self._stream)
         self._enqueue_boundary(self._F)
 
     def one_time_step(self):
@@ -482,10 +520,11 @@ class Simulation:
         for b in (self._F, self._Fnew, self._M):
             if b is not None:
                 b.free()
-        for _, il, st, rhs, _o in self._bc_dev:
-            il.free()
-            st.free()
-            rhs.free()
+        for _, dev in self._bc_dev:
+            for key, val in dev.items():
+                for b in (val if isinstance(val, list) else [val]):
+                    if isinstance(b, runtime.DeviceBuffer):
+                        b.free()
         self._bc_dev = []
         if self._stream:
             self._core.lbm_stream_destroy(self._stream)

@@ -1,0 +1,639 @@
+"""Scheme dictionaries of pylbm's demos whose results pylbm pins in tests/reference/*.h5.
+
+TEST INFRASTRUCTURE.  Each function restates, as a pylbm dictionary, the
+physics of one reference demo run by pylbm's own regression tests
+(tests/test_demo_1d.py, test_demo_2d.py, test_demo_3d.py): same lattice,
+moment basis, equilibrium, relaxation rates, initial state and boundary
+conditions, at the space step and final time those tests use.  The golden
+fields (converted from the reference's HDF5 files by
+golden/make_demo_golden.py) are compared at pylbm's own tolerance
+(tests/conftest.py:306-307: rel 1e-14, abs 1e-7).
+
+``bc`` defaults to pylbm_gb300.boundary; passing the reference's ``pylbm.bc``
+gives the dictionary pylbm itself accepts.
+"""
+import numpy as np
+import sympy as sp
+
+X, Y, Z, LA = sp.symbols("X, Y, Z, lambda")
+RHO, QX, QY = sp.symbols("rho, qx, qy")
+
+
+def _bc(bc):
+    if bc is None:
+        from pylbm_gb300 import boundary as bc
+    return bc
+
+
+def run_to(sim, final_time):
+    """Advance as the demos do: ``while sol.t < Tf: sol.one_time_step()``."""
+    while sim.t < final_time:
+        sim.one_time_step()
+    return sim
+
+
+def poiseuille(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Channel flow, D2Q9 MRT (demo/2D/Poiseuille.py:21-104).
+
+    Box [0, 2] x [-0.5, 0.5]; inflow (label 2) by Bouzidi bounce-back with
+    the parabolic profile and a linear pressure; outflow (label 1) NeumannX;
+    walls (label 0) Bouzidi bounce-back.
+    """
+    bc = _bc(bc)
+    la, width, height = 1.0, 2, 1
+    max_velocity, rhoo, mu, zeta = 0.1, 1.0, 0.00185, 1.0e-2
+    grad_pressure = -max_velocity * 8.0 / height**2 * 3.0 / (la**2 * rhoo) * mu
+    c = 3.0 / (la * rhoo * dx)
+    s1 = 1.0 / (0.5 + zeta * c)
+    s2 = 1.0 / (0.5 + mu * c)
+    inv = 1.0 / (LA**2 * rhoo)
+    qx2, qy2, qxy = inv * QX**2, inv * QY**2, inv * QX * QY
+    q2 = qx2 + qy2
+
+    def bc_in(f, m, x, y, width, height, max_velocity, grad_pressure):
+        m[RHO] = (x - 0.5 * width) * grad_pressure
+        m[QX] = max_velocity * (1.0 - 4.0 * y**2 / height**2)
+
+    return {
+        "box": {"x": [0.0, width], "y": [-0.5 * height, 0.5 * height], "label": [2, 1, 0, 0]},
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [{
+            "velocities": list(range(9)),
+            "polynomials": [1, LA * X, LA * Y, 3 * (X**2 + Y**2) - 4,
+                            0.5 * (9 * (X**2 + Y**2)**2 - 21 * (X**2 + Y**2) + 8),
+                            3 * X * (X**2 + Y**2) - 5 * X, 3 * Y * (X**2 + Y**2) - 5 * Y,
+                            X**2 - Y**2, X * Y],
+            "relaxation_parameters": [0.0, 0.0, 0.0, s1, s1, s1, s1, s2, s2],
+            "equilibrium": [RHO, QX, QY, -2 * RHO + 3 * q2, RHO - 3 * q2, -QX / LA, -QY / LA,
+                            qx2 - qy2, qxy],
+            "conserved_moments": [RHO, QX, QY],
+        }],
+        "parameters": {LA: la},
+        "init": {RHO: 1.0, QX: 0.0, QY: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack}},
+            1: {"method": {0: bc.NeumannX}},
+            2: {"method": {0: bc.BouzidiBounceBack},
+                "value": (bc_in, (width, height, max_velocity, grad_pressure))},
+        },
+        "generator": generator,
+    }
+
+
+def poiseuille_vec(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Channel flow with three coupled D2Q4 (demo/2D/Poiseuille_vec.py:48-130).
+
+    Box [0, 1] x [-0.25, 0.25]; p, ux, uy each carried by one D2Q4; Bouzidi
+    bounce-back / anti-bounce-back walls, pressure given at both ends.
+    """
+    bc = _bc(bc)
+    P, UX, UY = sp.symbols("p, ux, uy")
+    width, height, la = 1.0, 0.5, 1.0
+    max_velocity, mu, zeta, cte = 0.1, 0.00185, 1.0e-5, 3.0
+    grad_pressure = -mu * max_velocity * 8.0 / height**2
+    c = 3.0 / (la * dx)
+    s1 = 1.0 / (0.5 + zeta * c)
+    s2 = 1.0 / (0.5 + mu * c)
+    vel = list(range(1, 5))
+    polys = [1, LA * X, LA * Y, X**2 - Y**2]
+
+    def bc_in(f, m, x, y, width, height, max_velocity, grad_pressure, cte):
+        m[P] = (x - 0.5 * width) * grad_pressure * cte
+        m[UX] = max_velocity * (1.0 - 4.0 * y**2 / height**2)
+
+    def bc_out(f, m, x, y, width, grad_pressure, cte):
+        m[P] = (x - 0.5 * width) * grad_pressure * cte
+
+    return {
+        "box": {"x": [0.0, width], "y": [-0.5 * height, 0.5 * height], "label": [2, 1, 0, 0]},
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [
+            {"velocities": vel, "polynomials": polys, "relaxation_parameters": [0.0, s1, s1, 1.0],
+             "equilibrium": [P, UX, UY, 0.0], "conserved_moments": P},
+            {"velocities": vel, "polynomials": polys, "relaxation_parameters": [0.0, s2, s2, 1.0],
+             "equilibrium": [UX, UX**2 + P / cte, UX * UY, 0.0], "conserved_moments": UX},
+            {"velocities": vel, "polynomials": polys, "relaxation_parameters": [0.0, s2, s2, 1.0],
+             "equilibrium": [UY, UX * UY, UY**2 + P / cte, 0.0], "conserved_moments": UY},
+        ],
+        "parameters": {LA: la},
+        "init": {P: 0.0, UX: 0.0, UY: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack, 1: bc.BouzidiAntiBounceBack, 2: bc.BouzidiAntiBounceBack}},
+            1: {"method": {0: bc.BouzidiAntiBounceBack, 1: bc.NeumannX, 2: bc.NeumannX},
+                "value": (bc_out, (width, grad_pressure, cte))},
+            2: {"method": {0: bc.BouzidiAntiBounceBack, 1: bc.BouzidiAntiBounceBack, 2: bc.BouzidiAntiBounceBack},
+                "value": (bc_in, (width, height, max_velocity, grad_pressure, cte))},
+        },
+        "generator": generator,
+    }
+
+
+def orszag_tang(dx=2.0 * np.pi / 64, bc=None, generator="cuda"):
+    """Orszag-Tang vortex of 2D MHD, six coupled D2Q4 (demo/2D/Orszag_Tang_vortex.py:25-168).
+
+    Periodic [0, 2 pi]^2, la = 10, all relaxation rates 1.95.
+    """
+    GA = sp.Symbol("GA")
+    rho, qx, qy, E, Bx, By = sp.symbols("rho, qx, qy, E, Bx, By")
+    gamma, la = 5.0 / 3.0, 10.0
+    s0 = s1 = s2 = s3 = 1.95
+    p = (GA - 1) * (E - (qx**2 + qy**2) / (2 * rho) - (Bx**2 + By**2) / 2)
+    ps = p + (Bx**2 + By**2) / 2
+    vB = (qx * Bx + qy * By) / rho
+    vel, polys = list(range(1, 5)), [1, LA * X, LA * Y, X**2 - Y**2]
+
+    def init_rho(x, y, gamma):
+        return gamma**2 * np.ones(x.shape)
+
+    def init_qx(x, y, gamma):
+        return -(gamma**2) * np.sin(y)
+
+    def init_qy(x, y, gamma):
+        return gamma**2 * np.sin(x)
+
+    def init_bx(x, y):
+        return -np.sin(y)
+
+    def init_by(x, y):
+        return np.sin(2 * x)
+
+    def init_e(x, y, gamma):
+        kinetic = 0.5 * (init_qx(x, y, gamma)**2 + init_qy(x, y, gamma)**2) / init_rho(x, y, gamma)
+        magnetic = 0.5 * (init_bx(x, y)**2 + init_by(x, y)**2)
+        return kinetic + magnetic + gamma / (gamma - 1)
+
+    def scheme(cons, rates, eq):
+        return {"velocities": vel, "conserved_moments": cons, "polynomials": polys,
+                "relaxation_parameters": rates, "equilibrium": eq}
+
+    return {
+        "box": {"x": [0.0, 2 * np.pi], "y": [0.0, 2 * np.pi], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [
+            scheme(rho, [0.0, s1, s1, s0], [rho, qx, qy, 0.0]),
+            scheme(qx, [0.0, s2, s2, s0], [qx, qx**2 / rho + ps - Bx**2, qx * qy / rho - Bx * By, 0.0]),
+            scheme(qy, [0.0, s2, s2, s0], [qy, qx * qy / rho - Bx * By, qy**2 / rho + ps - By**2, 0.0]),
+            scheme(E, [0.0, s3, s3, s0], [E, (E + ps) * qx / rho - vB * Bx, (E + ps) * qy / rho - vB * By, 0.0]),
+            scheme(Bx, [0.0, s3, s3, s0], [Bx, 0, (qy * Bx - qx * By) / rho, 0.0]),
+            scheme(By, [0.0, s3, s3, s0], [By, (qx * By - qy * Bx) / rho, 0, 0.0]),
+        ],
+        "init": {rho: (init_rho, (gamma,)), qx: (init_qx, (gamma,)), qy: (init_qy, (gamma,)),
+                 E: (init_e, (gamma,)), Bx: init_bx, By: init_by},
+        "parameters": {LA: la, GA: gamma},
+        "generator": generator,
+    }
+
+
+def advection_3d(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Advection on the 3D torus, D3Q6 (demo/3D/advection.py:30-91): c = (0.5, 0.2, 0.1), s = 1."""
+    U = sp.Symbol("u")
+    ux, uy, uz, s, la = 0.5, 0.2, 0.1, 1.0, 1.0
+
+    def u0(x, y, z):
+        return 0.5 * np.ones((x.size, y.size, z.size)) + 0.5 * (
+            ((x - 0.5)**2 + (y - 0.5)**2 + (z - 0.5)**2) < 0.25**2)
+
+    return {
+        "box": {"x": [0.0, 1.0], "y": [0.0, 1.0], "z": [0.0, 1.0], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [{
+            "velocities": list(range(1, 7)),
+            "conserved_moments": [U],
+            "polynomials": [1, LA * X, LA * Y, LA * Z, X**2 - Y**2, X**2 - Z**2],
+            "equilibrium": [U, ux * U, uy * U, uz * U, 0.0, 0.0],
+            "relaxation_parameters": [0.0, s, s, s, s, s],
+        }],
+        "init": {U: u0},
+        "parameters": {LA: la},
+        "generator": generator,
+    }
+
+
+def reduce_field(a):
+    """What a fixture keeps of a field: all of it up to 65 536 nodes; beyond,
+    the middle z-plane, every 4th node and the sum (the reference's 64^3
+    files are 2 MB)."""
+    a = np.asarray(a, dtype=np.float64)
+    if a.size <= 65536:
+        return {"": a}
+    return {"__mid": np.ascontiguousarray(a[:, :, a.shape[2] // 2]),
+            "__every4": np.ascontiguousarray(a[::4, ::4, ::4]), "__sum": np.array(a.sum())}
+
+
+def poiseuille_3d(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Channel flow with four coupled D3Q6 (demo/3D/poiseuille.py:60-155).
+
+    Box [0, 1] x [-0.25, 0.25] x [-2 dx, 2 dx], periodic in z; Bouzidi walls,
+    pressure given at both ends (outflow NeumannX for the velocities).
+    """
+    bc = _bc(bc)
+    P, UX, UY, UZ = sp.symbols("p,ux,uy,uz")
+    width, height, la = 1.0, 0.5, 1.0
+    max_velocity, mu, cte = 0.1, 1.0e-3, 10.0
+    grad_pressure = -mu * max_velocity * 8.0 / height**2
+    s = 1.0 / (0.5 + 1.0 / np.sqrt(12))
+    rates = [0.0, s, s, s, s, s]
+    vel = list(range(1, 7))
+    polys = [1, LA * X, LA * Y, LA * Z, X**2 - Y**2, X**2 - Z**2]
+
+    def bc_in(f, m, x, y, z):
+        m[P] = (x - 0.5 * width) * grad_pressure * cte
+        m[UX] = max_velocity * (1.0 - 4.0 * y**2 / height**2)
+
+    def bc_out(f, m, x, y, z):
+        m[P] = (x - 0.5 * width) * grad_pressure * cte
+
+    def scheme(cons, eq):
+        return {"velocities": vel, "conserved_moments": cons, "polynomials": polys,
+                "relaxation_parameters": rates, "equilibrium": eq}
+
+    walls = {0: bc.BouzidiBounceBack, 1: bc.BouzidiAntiBounceBack, 2: bc.BouzidiAntiBounceBack,
+             3: bc.BouzidiAntiBounceBack}
+    return {
+        "box": {"x": [0.0, width], "y": [-0.5 * height, 0.5 * height], "z": [-2 * dx, 2 * dx],
+                "label": [1, 2, 0, 0, -1, -1]},
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [
+            scheme(P, [P, UX, UY, UZ, 0.0, 0.0]),
+            scheme(UX, [UX, UX**2 + P / cte, UX * UY, UX * UZ, 0.0, 0.0]),
+            scheme(UY, [UY, UY * UX, UY**2 + P / cte, UY * UZ, 0.0, 0.0]),
+            scheme(UZ, [UZ, UZ * UX, UZ * UY, UZ**2 + P / cte, 0.0, 0.0]),
+        ],
+        "init": {P: 0.0, UX: 0.0, UY: 0.0, UZ: 0.0},
+        "boundary_conditions": {
+            0: {"method": walls},
+            1: {"method": {0: bc.BouzidiAntiBounceBack, 1: bc.NeumannX, 2: bc.NeumannX, 3: bc.NeumannX},
+                "value": bc_out},
+            2: {"method": {0: bc.BouzidiAntiBounceBack, 1: bc.BouzidiAntiBounceBack, 2: bc.BouzidiAntiBounceBack,
+                           3: bc.BouzidiAntiBounceBack},
+                "value": bc_in},
+        },
+        "parameters": {LA: la},
+        "generator": generator,
+    }
+
+
+def euler_1d(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Sod shock tube, three coupled D1Q2 (demo/1D/euler.py:45-118): la = 3, Neumann ends."""
+    bc = _bc(bc)
+    rho, q, E = sp.symbols("rho, q, E")
+    la_c = sp.symbols("lambda", constants=True)
+    gamma, xmin, xmax, la = 1.4, 0.0, 1.0, 3.0
+    rho_l, rho_r, p_l, p_r, u_l, u_r = 1.0, 1.0 / 8.0, 1.0, 0.1, 0.0, 0.0
+    q_l, q_r = rho_l * u_l, rho_r * u_r
+    e_l = rho_l * u_l**2 + p_l / (gamma - 1.0)
+    e_r = rho_r * u_r**2 + p_r / (gamma - 1.0)
+
+    def riemann(x, xmin, xmax, left, right):
+        xm = 0.5 * (xmin + xmax)
+        u = np.empty(x.shape)
+        u[x < xm] = left
+        u[x == xm] = 0.5 * (left + right)
+        u[x > xm] = right
+        return u
+
+    def scheme(cons, rate, flux):
+        return {"velocities": [1, 2], "conserved_moments": cons, "polynomials": [1, la_c * X],
+                "relaxation_parameters": [0, rate], "equilibrium": [cons, flux]}
+
+    return {
+        "box": {"x": [xmin, xmax], "label": 0},
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [
+            scheme(rho, 1.9, q),
+            scheme(q, 1.5, (gamma - 1.0) * E + 0.5 * (3.0 - gamma) * q**2 / rho),
+            scheme(E, 1.4, gamma * E * q / rho - 0.5 * (gamma - 1.0) * q**3 / rho**2),
+        ],
+        "init": {rho: (riemann, (xmin, xmax, rho_l, rho_r)), q: (riemann, (xmin, xmax, q_l, q_r)),
+                 E: (riemann, (xmin, xmax, e_l, e_r))},
+        "boundary_conditions": {0: {"method": {0: bc.Neumann, 1: bc.Neumann, 2: bc.Neumann}}},
+        "parameters": {la_c: la},
+        "generator": generator,
+    }
+
+
+def lid_driven_cavity(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Lid-driven cavity, D2Q9 Geier scheme with relative velocity
+    (demo/2D/lid_driven_cavity.py:57-229, scheme_name "Geier").
+
+    Bouzidi bounce-back walls; the lid (label 1) moves at 0.05.
+    """
+    bc = _bc(bc)
+    la_c = sp.symbols("lambda", constants=True)
+    la, rho_o, driven_velocity, mu = 1.0, 1.0, 0.05, 5.0e-6
+    zeta = 100 * mu
+    ux, uy = QX / RHO, QY / RHO
+    rhou2 = RHO * (ux**2 + uy**2)
+    c = 3.0 / (la * rho_o * dx)
+    s_1 = 1 / (0.5 + c * (zeta - 2 * mu / 3))
+    s_2 = 1 / (0.5 + c * mu)
+
+    def bc_up(f, m, x, y, rho_o, driven_velocity):
+        m[RHO] = rho_o
+        m[QX] = rho_o * driven_velocity
+        m[QY] = 0.0
+
+    return {
+        "parameters": {la_c: la},
+        "box": {"x": [0.0, 1.0], "y": [0.0, 1.0], "label": [0, 0, 0, 1]},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [{
+            "velocities": list(range(9)),
+            "polynomials": [1, X, Y, X**2 + Y**2, X * Y**2, Y * X**2, X**2 * Y**2, X**2 - Y**2, X * Y],
+            "relaxation_parameters": [0.0, 0.0, 0.0, s_1, s_1, s_1, s_1, s_2, s_2],
+            "equilibrium": [RHO, QX, QY, rhou2 + 2 / 3 * RHO * la_c**2, QX * (la_c**2 / 3 + uy**2),
+                            QY * (la_c**2 / 3 + ux**2), RHO * (la_c**2 / 3 + ux**2) * (la_c**2 / 3 + uy**2),
+                            RHO * (ux**2 - uy**2), RHO * ux * uy],
+            "conserved_moments": [RHO, QX, QY],
+        }],
+        "init": {RHO: rho_o, QX: 0.0, QY: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack}},
+            1: {"method": {0: bc.BouzidiBounceBack}, "value": (bc_up, (rho_o, driven_velocity))},
+        },
+        "generator": generator,
+        "relative_velocity": [QX / RHO, QY / RHO],
+    }
+
+
+def _geier(la_c, dx, la, rho_o, mu, zeta):
+    """D2Q9 Geier basis, equilibrium and rates (moments_choice "Geier" of the 2D Navier-Stokes demos)."""
+    ux, uy = QX / RHO, QY / RHO
+    rhou2 = RHO * (ux**2 + uy**2)
+    c = 3.0 / (la * rho_o * dx)
+    s_1 = 1 / (0.5 + c * (zeta - 2 * mu / 3))
+    s_2 = 1 / (0.5 + c * mu)
+    return {
+        "velocities": list(range(9)),
+        "polynomials": [1, X, Y, X**2 + Y**2, X * Y**2, Y * X**2, X**2 * Y**2, X**2 - Y**2, X * Y],
+        "relaxation_parameters": [0.0, 0.0, 0.0, s_1, s_1, s_1, s_1, s_2, s_2],
+        "equilibrium": [RHO, QX, QY, rhou2 + 2 / 3 * RHO * la_c**2, QX * (la_c**2 / 3 + uy**2),
+                        QY * (la_c**2 / 3 + ux**2), RHO * (la_c**2 / 3 + ux**2) * (la_c**2 / 3 + uy**2),
+                        RHO * (ux**2 - uy**2), RHO * ux * uy],
+        "conserved_moments": [RHO, QX, QY],
+    }
+
+
+def kelvin_helmholtz(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Periodic double shear layer, D2Q9 Geier with relative velocity
+    (demo/2D/Kelvin_Helmoltz.py:44-219): Mach 0.1 (la = sqrt(3)/0.1), k = 80, delta = 0.05."""
+    la_c = sp.symbols("lambda", constants=True)
+    la, rho_o, u_o, zeta, mu, k, delta = np.sqrt(3) / 0.1, 1.0, 0.5, 0.0366, 1.0e-6, 80, 0.05
+
+    def qx_init(x, y, U, k):
+        return np.zeros_like(x) + U * np.tanh(k * (y - 0.25)) * (y <= 0.5) + U * np.tanh(k * (0.75 - y)) * (y > 0.5)
+
+    def qy_init(x, y, U, delta):
+        return np.zeros_like(y) + U * delta * np.sin(2 * np.pi * (x + 0.25))
+
+    return {
+        "parameters": {la_c: la},
+        "box": {"x": [0.0, 1.0], "y": [0.0, 1.0], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [_geier(la_c, dx, la, rho_o, mu, zeta)],
+        "init": {RHO: rho_o, QX: (qx_init, (u_o, k)), QY: (qy_init, (u_o, delta))},
+        "relative_velocity": [QX / RHO, QY / RHO],
+        "generator": generator,
+    }
+
+
+def karman_vortex_street(dx=1.0 / 64, bc=None, circle=None, generator="cuda"):
+    """Flow past a disc, D2Q9 Geier with relative velocity (demo/2D/Karman_vortex_street.py:49-225).
+
+    Box [0, 2] x [0, 1]; label 0 (inflow and channel walls) Bouzidi
+    bounce-back with the inflow state, label 1 NeumannX, disc (label 2,
+    radius 1/32 at (0.3, 0.5 + 2 dx)) Bouzidi bounce-back.
+    """
+    bc = _bc(bc)
+    if circle is None:
+        from pylbm_gb300.geometry import Circle as circle
+    la_c = sp.symbols("lambda", constants=True)
+    la, rho_o, u_o, mu, radius = 1.0, 1.0, 0.05, 5.0e-6, 1.0 / 32
+    zeta = 10 * mu
+
+    def bc_in(f, m, x, y, rho_o, u_o):
+        m[RHO] = rho_o
+        m[QX] = rho_o * u_o
+        m[QY] = 0.0
+
+    return {
+        "box": {"x": [0.0, 2.0], "y": [0.0, 1.0], "label": [0, 1, 0, 0]},
+        "elements": [circle([0.3, 0.5 + 2 * dx], radius, label=2)],
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [_geier(la_c, dx, la, rho_o, mu, zeta)],
+        "parameters": {la_c: la},
+        "init": {RHO: rho_o, QX: rho_o * u_o, QY: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack}, "value": (bc_in, (rho_o, u_o))},
+            1: {"method": {0: bc.NeumannX}},
+            2: {"method": {0: bc.BouzidiBounceBack}},
+        },
+        "generator": generator,
+        "relative_velocity": [QX / RHO, QY / RHO],
+    }
+
+
+def advection_2d(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Advection on the torus, D2Q4 with a constant relative velocity (demo/2D/advection.py:21-115).
+
+    c = (0.2, 0.5), la = 2, rates given through the parameters sigma_0, sigma_1.
+    """
+    U = sp.Symbol("U")
+    CX, CY, la_c = sp.symbols("c_0, c_1, lambda", constants=True)
+    sigma0, sigma1 = sp.symbols("sigma_0, sigma_1", constants=True)
+    xmin, xmax, ymin, ymax = 0.0, 1.0, 0.0, 1.0
+    sq, sxy = 1 / (0.5 + sigma0), 1 / (0.5 + sigma1)
+
+    def u_init(x, y, xmin, xmax, ymin, ymax):
+        center = (0.75 * xmin + 0.25 * xmax, 0.50 * ymin + 0.50 * ymax)
+        return 1 + 0.5 * ((x - center[0])**2 + (y - center[1])**2 < 0.1**2)
+
+    return {
+        "box": {"x": [xmin, xmax], "y": [ymin, ymax], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [{
+            "velocities": list(range(1, 5)),
+            "conserved_moments": U,
+            "polynomials": [1, X, Y, X**2 - Y**2],
+            "relaxation_parameters": [0.0, sq, sq, sxy],
+            "equilibrium": [U, CX * U, CY * U, 0],
+        }],
+        "init": {U: (u_init, (xmin, xmax, ymin, ymax))},
+        "generator": generator,
+        "parameters": {la_c: 2.0, CX: 0.2, CY: 0.5, sigma0: 1.0e-2, sigma1: 0.5},
+        "relative_velocity": [CX, CY],
+    }
+
+
+def air_conditioning(dx=1.0 / 64, bc=None, parallelogram=None, generator="cuda"):
+    """Buoyant flow with a cold inflow: D2Q9 MRT for (rho, q) with the buoyancy
+    source term on qy, coupled to a D2Q5 for T (demo/2D/air_conditioning.py:36-158).
+
+    Two solid blocks (parallelograms) at the bottom corners; label 0 walls
+    and label 1 inflow by Bouzidi bounce-back (flow) / anti-bounce-back (T),
+    label 2 NeumannX.
+    """
+    bc = _bc(bc)
+    if parallelogram is None:
+        from pylbm_gb300.geometry import Parallelogram as parallelogram
+    rho, qx, qy, T = sp.symbols("rho, qx, qy, T")
+    T0, Tin = 0.5, -0.5
+    xmin, xmax, ymin, ymax = 0.0, 1.0, 0.0, 1.0
+    Ra, Pr, alpha, la, rhoo, g, uo = 2000, 0.71, 0.005, 1.0, 1.0, 9.81, 0.025
+    nu = np.sqrt(Pr * alpha * 9.81 * (T0 - Tin) * (ymax - ymin) / Ra)
+    kappa = nu / Pr
+    eta = nu
+    snu = 1.0 / (0.5 + 3 * nu)
+    seta = 1.0 / (0.5 + 3 * eta)
+    sq = 8 * (2 - snu) / (8 - snu)
+    se = seta
+    sf = [0.0, 0.0, 0.0, seta, se, sq, sq, snu, snu]
+    a = 0.5
+    skappa = 1.0 / (0.5 + 10 * kappa / (4 + a))
+    se = 1.0 / (0.5 + np.sqrt(3) / 3)
+    snu = se
+    sT = [0.0, skappa, skappa, se, snu]
+
+    def init_T(x, y, T0):
+        return T0
+
+    def bc_wall(f, m, x, y, T0):
+        m[qx] = 0.0
+        m[qy] = 0.0
+        m[T] = T0
+
+    def bc_in(f, m, x, y, T0, Tin, ymax, rhoo, uo):
+        m[qx] = rhoo * uo
+        m[qy] = 0.0
+        m[T] = T0 + (Tin - T0) * (ymax - y) * (y - 0.8) * 100
+
+    return {
+        "box": {"x": [xmin, xmax], "y": [ymin, ymax], "label": [1, 2, 0, 0]},
+        "elements": [parallelogram([xmin, ymin], [0.1, 0], [0, 0.8], label=0),
+                     parallelogram([xmax, ymin], [-0.1, 0], [0, 0.8], label=0)],
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [
+            {"velocities": list(range(9)), "conserved_moments": [rho, qx, qy],
+             "polynomials": [1, X, Y, 3 * (X**2 + Y**2) - 4,
+                             sp.Rational(1, 2) * (9 * (X**2 + Y**2)**2 - 21 * (X**2 + Y**2) + 8),
+                             3 * X * (X**2 + Y**2) - 5 * X, 3 * Y * (X**2 + Y**2) - 5 * Y, X**2 - Y**2, X * Y],
+             "relaxation_parameters": sf,
+             "equilibrium": [rho, qx, qy, -2 * rho + 3 * (qx**2 + qy**2), rho - 3 * (qx**2 + qy**2), -qx, -qy,
+                             qx**2 - qy**2, qx * qy],
+             "source_terms": {qy: alpha * g * T}},
+            {"velocities": list(range(5)), "conserved_moments": T,
+             "polynomials": [1, X, Y, 5 * (X**2 + Y**2) - 4, (X**2 - Y**2)],
+             "equilibrium": [T, T * qx, T * qy, a * T, 0.0], "relaxation_parameters": sT},
+        ],
+        "init": {rho: 1.0, qx: 0.0, qy: 0.0, T: (init_T, (T0,))},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack, 1: bc.BouzidiAntiBounceBack}, "value": (bc_wall, (T0,))},
+            1: {"method": {0: bc.BouzidiBounceBack, 1: bc.BouzidiAntiBounceBack},
+                "value": (bc_in, (T0, Tin, ymax, rhoo, uo))},
+            2: {"method": {0: bc.NeumannX, 1: bc.NeumannX}},
+        },
+        "generator": generator,
+    }
+
+
+def rayleigh_benard(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Rayleigh-Benard convection: D2Q9 MRT with buoyancy source on qy coupled
+    to a D2Q5 for T (demo/2D/Rayleigh-Benard.py:87-206, time_bc=True).
+
+    Periodic in x; bottom wall (label 0) with a bottom temperature that
+    switches every 5 time units (time-dependent boundary value), top wall
+    (label 1); Bouzidi bounce-back (flow) / anti-bounce-back (T).
+    """
+    bc = _bc(bc)
+    la_c = sp.symbols("lambda")
+    rho, qx, qy, T = sp.symbols("rho, qx, qy, T")
+    Td, Tu = 0.5, -0.5
+    xmin, xmax, ymin, ymax = 0.0, 2.0, 0.0, 1.0
+    Ra, Pr, alpha, la, g = 2000, 0.71, 0.005, 1.0, 9.81
+    nu = np.sqrt(Pr * alpha * 9.81 * (Td - Tu) * (ymax - ymin) / Ra)
+    kappa = nu / Pr
+    eta = nu
+    snu = 1.0 / (0.5 + 3 * nu)
+    seta = 1.0 / (0.5 + 3 * eta)
+    sq = 8 * (2 - snu) / (8 - snu)
+    se = seta
+    sf = [0.0, 0.0, 0.0, seta, se, sq, sq, snu, snu]
+    a = 0.5
+    skappa = 1.0 / (0.5 + 10 * kappa / (4 + a))
+    se = 1.0 / (0.5 + np.sqrt(3) / 3)
+    snu = se
+    sT = [0.0, skappa, skappa, se, snu]
+
+    def init_T(x, y, Td, Tu, xmin, xmax, ymin, ymax):
+        xmid, ymid = (xmax + xmin) / 2, (ymax + ymin) / 2
+        return Td + (Tu - Td) / (ymax - ymin) * (y - ymin) + Td * (x < 1.1 * xmid) * (x > 0.9 * xmid) * (y < ymid)
+
+    def bc_up(f, m, x, y, Tu):
+        m[qx] = 0.0
+        m[qy] = 0.0
+        m[T] = Tu
+
+    def bc_down_with_time(f, m, t, x, y, Td, Tu):
+        m[qx] = 0.0
+        m[qy] = 0.0
+        if 0 <= t % 10.0 <= 5:
+            m[T] = Td
+        else:
+            m[T] = Tu
+
+    walls = {0: bc.BouzidiBounceBack, 1: bc.BouzidiAntiBounceBack}
+    return {
+        "box": {"x": [xmin, xmax], "y": [ymin, ymax], "label": [-1, -1, 0, 1]},
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [
+            {"velocities": list(range(9)), "conserved_moments": [rho, qx, qy],
+             "polynomials": [1, X, Y, 3 * (X**2 + Y**2) - 4, 0.5 * (9 * (X**2 + Y**2)**2 - 21 * (X**2 + Y**2) + 8),
+                             3 * X * (X**2 + Y**2) - 5 * X, 3 * Y * (X**2 + Y**2) - 5 * Y, X**2 - Y**2, X * Y],
+             "relaxation_parameters": sf,
+             "equilibrium": [rho, qx, qy, -2 * rho + 3 * (qx**2 + qy**2), rho - 3 * (qx**2 + qy**2), -qx, -qy,
+                             qx**2 - qy**2, qx * qy],
+             "source_terms": {qy: alpha * g * T}},
+            {"velocities": list(range(5)), "conserved_moments": T,
+             "polynomials": [1, X, Y, 5 * (X**2 + Y**2) - 4, (X**2 - Y**2)],
+             "equilibrium": [T, T * qx, T * qy, a * T, 0.0], "relaxation_parameters": sT},
+        ],
+        "init": {rho: 1.0, qx: 0.0, qy: 0.0, T: (init_T, (Td, Tu, xmin, xmax, ymin, ymax))},
+        "boundary_conditions": {
+            0: {"method": dict(walls), "value": (bc_down_with_time, (Td, Tu)), "time_bc": True},
+            1: {"method": dict(walls), "value": (bc_up, (Tu,))},
+        },
+        "generator": generator,
+    }
+
+
+# name: (dictionary builder, final time, golden file, {golden field: conserved moment name})
+CASES = {
+    "poiseuille": (poiseuille, 0.5, "test2D_poiseuille", {"rho": "rho", "qx": "qx", "qy": "qy"}),
+    "poiseuille_vec": (poiseuille_vec, 0.5, "test2D_poiseuille_vec", {"p": "p", "ux": "ux", "uy": "uy"}),
+    "orszag_tang": (orszag_tang, 0.5, "test2D_orszag_Tang_vortex",
+                    {k: k for k in ("rho", "qx", "qy", "E", "Bx", "By")}),
+    "advection_3d": (advection_3d, 0.5, "test3D_advection", {"u": "u"}),
+    "lid_driven_cavity": (lid_driven_cavity, 0.5, "test2D_lid_driven_cavity", {"rho": "rho", "qx": "qx", "qy": "qy"}),
+    "kelvin_helmholtz": (kelvin_helmholtz, 0.5, "test2D_kelvin_Helmoltz", {"rho": "rho", "qx": "qx", "qy": "qy"}),
+    "karman_vortex_street": (karman_vortex_street, 0.5, "test2D_karman_vortex_street",
+                             {"rho": "rho", "qx": "qx", "qy": "qy"}),
+    "advection_2d": (advection_2d, 0.5, "test2D_advection", {"U": "U"}),
+    "air_conditioning": (air_conditioning, 0.5, "test2D_air_conditioning",
+                         {"rho": "rho", "qx": "qx", "qy": "qy", "T": "T"}),
+    "rayleigh_benard": (rayleigh_benard, 0.5, "test2D_rayleigh_benard",
+                        {"rho": "rho", "qx": "qx", "qy": "qy", "T": "T"}),
+    "euler_1d": (euler_1d, 0.5, "test1D_euler", {"rho": "rho", "q": "q", "E": "E"}),
+    "poiseuille_3d": (poiseuille_3d, 0.5, "test3D_poseuille", {"p": "p", "ux": "ux", "uy": "uy", "uz": "uz"}),
+}

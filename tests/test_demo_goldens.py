@@ -1,0 +1,46 @@
+"""pylbm's own golden demo results (tests/reference/*.h5) against the CPU oracle.
+
+The fixtures hold the reference's HDF5 fields at the final time of pylbm's
+regression tests (tests/golden/make_demo_golden.py, which also checks that
+the reference itself reproduces them from the restated dictionaries of
+tests/demo_cases.py).  Tolerance: pylbm's own (tests/conftest.py:306-307).
+"""
+import numpy as np
+import pytest
+import sympy as sp
+
+import demo_cases
+from conftest import golden
+from oracle import OracleSimulation
+
+
+def conserved_fields(sim, moments, fields, mask):
+    out = {}
+    for key, cons in fields.items():
+        v = np.array(moments[sim.scheme.consm[sp.Symbol(cons)]], dtype=np.float64)
+        if mask.ndim:
+            v[~mask] = 0.0
+        else:
+            assert bool(mask)  # 3D fixtures: every node is fluid
+        out[key] = v
+    return out
+
+
+def assert_golden(values, g, fields):
+    for key in fields:
+        for suffix, part in demo_cases.reduce_field(values[key]).items():
+            ref = g[key + suffix]
+            tol = 1e-7 if suffix != "__sum" else 1e-7 * values[key].size
+            diff = np.abs(part - ref)
+            assert np.all(diff <= np.maximum(1e-14 * np.abs(ref), tol)), (key + suffix, float(diff.max()))
+
+
+@pytest.mark.parametrize("name", list(demo_cases.CASES))
+def test_oracle_reproduces_reference_golden(name):
+    build, final_time, _, fields = demo_cases.CASES[name]
+    g = golden(f"demo_{name}.npz")
+    o = OracleSimulation(build())
+    demo_cases.run_to(o, final_time)
+    assert o.nt == int(g["steps"])
+    vals = conserved_fields(o, o.moments(), fields, g["mask"])
+    assert_golden(vals, g, fields)

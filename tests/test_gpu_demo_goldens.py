@@ -1,0 +1,30 @@
+"""pylbm's own golden demo results through generator='cuda' (float64 on the GPU).
+
+Same fixtures and tolerance as test_demo_goldens.py (the CPU oracle); the GPU
+run must also stay within round-off of the oracle on every moment.
+"""
+import numpy as np
+import pytest
+
+import demo_cases
+from conftest import golden, rel_err
+from oracle import OracleSimulation
+from pylbm_gb300 import Simulation
+from test_demo_goldens import assert_golden, conserved_fields
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", list(demo_cases.CASES))
+def test_cuda_reproduces_reference_golden(name):
+    build, final_time, _, fields = demo_cases.CASES[name]
+    g = golden(f"demo_{name}.npz")
+    sim = Simulation(build())
+    demo_cases.run_to(sim, final_time)
+    assert sim.nt == int(g["steps"])
+    m = np.array([sim.m[k] for k in range(sim.scheme.nv)])
+    assert_golden(conserved_fields(sim, m, fields, g["mask"]), g, fields)
+    o = OracleSimulation(build())
+    demo_cases.run_to(o, final_time)
+    assert rel_err(m, o.moments()).max() < 1e-12
+    sim.free()

@@ -9,6 +9,7 @@ import os
 import re
 
 import numpy as np
+import sympy as sp
 import pytest
 
 from conftest import ROOT, golden
@@ -94,9 +95,37 @@ def test_domain_flags_match_reference():
 
 def test_unsupported_scheme_is_rejected():
     d = W.cavity(n=8)
-    d["relative_velocity"] = [W.QX / W.RHO, W.QY / W.RHO]
+    d["schemes"][0]["source_terms"] = {W.QX: W.RHO * sp.Symbol("X")}  # space-dependent source
     with pytest.raises(SchemeError):
         Scheme(d)
+    d = W.cavity(n=8)
+    d["relative_velocity"] = [W.QX / W.RHO]  # one component for two dimensions
+    with pytest.raises(SchemeError):
+        Scheme(d)
+
+
+def test_relative_velocity_translation_matrix():
+    """T(0) = I and T(u) T(-u) = I (pylbm/scheme.py:534-543); conserved rows first."""
+    d = W.cavity(n=8)
+    d["relative_velocity"] = [W.QX / W.RHO, W.QY / W.RHO]
+    sc = Scheme(d)
+    u = sc.rel_vel_symbols
+    assert sc.Tu.subs({u[0]: 0, u[1]: 0}) == sp.eye(9)
+    assert (sc.Tu * sc.Tmu).applyfunc(sp.expand) == sp.eye(9)
+    assert sc.Tu[1, 0] == -u[0] and sc.Tu[2, 0] == -u[1]  # qx - ux rho, qy - uy rho
+    src = SchemeSource(sc, shifted=False)
+    assert src.absolute_collide and "mc_rel" in src.header()
+    with pytest.raises(SchemeError):
+        SchemeSource(sc, shifted=False, style="reference")
+
+
+def test_source_terms_add_the_time_step_parameter():
+    d = W.cavity(n=8)
+    d["schemes"][0]["source_terms"] = {W.QY: -W.RHO * 0.01}
+    sc = Scheme(d)
+    assert [str(s) for s in sc.free_symbols] == ["dt"]
+    (k, rhs), = sc.source_terms
+    assert k == 2 and rhs == -0.01 * W.RHO
 
 
 def test_shifted_source_cancels_reference_state():
@@ -205,7 +234,9 @@ def test_fast_and_reference_styles_share_constants():
     sc = Scheme(W.cavity(n=8))
     fast = SchemeSource(sc, shifted=False)
     ref = SchemeSource(sc, shifted=False, style="reference")
-    assert ref.nvcc_flags == ["-fmad=false"] and fast.nvcc_flags == []
+    # both styles forbid implicit contraction; the fast one fuses explicitly
+    assert ref.nvcc_flags == ["-fmad=false"] and fast.nvcc_flags == ["-fmad=false"]
+    assert "lbm_fma<R>" in fast.header() and "lbm_fma" not in ref.header()
     assert "0.666666666666667" in ref.header()
     with pytest.raises(SchemeError):
         SchemeSource(sc, shifted=True, c0=[1, 0, 0], style="reference")
