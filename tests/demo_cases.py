@@ -12,6 +12,8 @@ golden/make_demo_golden.py) are compared at pylbm's own tolerance
 ``bc`` defaults to pylbm_gb300.boundary; passing the reference's ``pylbm.bc``
 gives the dictionary pylbm itself accepts.
 """
+import math
+
 import numpy as np
 import sympy as sp
 
@@ -214,12 +216,15 @@ def advection_3d(dx=1.0 / 64, bc=None, generator="cuda"):
 
 
 def reduce_field(a):
-    """What a fixture keeps of a field: all of it up to 65 536 nodes; beyond,
-    the middle z-plane, every 4th node and the sum (the reference's 64^3
-    files are 2 MB)."""
+    """What a fixture keeps of a field: all of it up to 8192 nodes; beyond, in
+    2D every 2nd node, the middle row and the sum, in 3D the middle z-plane,
+    every 4th node and the sum (the reference's 64^3 files are 2 MB)."""
     a = np.asarray(a, dtype=np.float64)
-    if a.size <= 65536:
+    if a.size <= 8192:
         return {"": a}
+    if a.ndim == 2:
+        return {"__every2": np.ascontiguousarray(a[::2, ::2]), "__midrow": np.ascontiguousarray(a[a.shape[0] // 2]),
+                "__sum": np.array(a.sum())}
     return {"__mid": np.ascontiguousarray(a[:, :, a.shape[2] // 2]),
             "__every4": np.ascontiguousarray(a[::4, ::4, ::4]), "__sum": np.array(a.sum())}
 
@@ -618,6 +623,121 @@ def rayleigh_benard(dx=1.0 / 64, bc=None, generator="cuda"):
     }
 
 
+def _bump(x, xmin, xmax, reg):
+    """Compactly supported bump of regularity ``reg`` centred at a quarter of
+    the domain (u_init of demo/1D/advection.py and demo/1D/burgers.py)."""
+    middle, width = 0.75 * xmin + 0.25 * xmax, 0.125 * (xmax - xmin)
+    coeffs = [(-1)**k * math.comb(reg, k) / (2 * k + 1) for k in range(reg + 1)]
+    cte = sum(coeffs)
+    out = np.zeros(x.shape)
+    left = (x > middle - width) & (x <= middle)
+    right = (x < middle + width) & (x > middle)
+    sl = (x[left] - (middle - width) - 0.5 * width) / (0.5 * width)
+    sr = (x[right] - middle - 0.5 * width) / (0.5 * width)
+    out[left] = sum(c * sl**(2 * k + 1) for k, c in enumerate(coeffs)) + cte
+    out[right] = cte - sum(c * sr**(2 * k + 1) for k, c in enumerate(coeffs))
+    return out / (2 * cte)
+
+
+def advection_1d(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Periodic advection, D1Q2 with a symbolic rate (demo/1D/advection.py:81-112, the D1Q2 run)."""
+    U, Xs = sp.symbols("u, X")
+    C, la_c = sp.symbols("c, lambda", constants=True)
+    sigma0 = sp.Symbol("sigma_0", constants=True)
+    return {
+        "box": {"x": [0.0, 1.0], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [{"velocities": [1, 2], "conserved_moments": U, "polynomials": [1, Xs],
+                     "relaxation_parameters": [0.0, 1 / (0.5 + sigma0)], "equilibrium": [U, C * U]}],
+        "init": {U: (_bump, (0.0, 1.0, 0))},
+        "generator": generator,
+        "parameters": {la_c: 1.0, C: 0.25, sigma0: 1 / 2.0 - 0.5},
+    }
+
+
+def burgers_1d(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Burgers equation, D1Q2 with Neumann ends (demo/1D/burgers.py:82-113, the D1Q2 run)."""
+    bc = _bc(bc)
+    U, Xs = sp.symbols("u, X")
+    la_c = sp.symbols("lambda", constants=True)
+    sigma0 = sp.Symbol("sigma_0", constants=True)
+    return {
+        "box": {"x": [-1.0, 1.0], "label": 0},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [{"velocities": [1, 2], "conserved_moments": U, "polynomials": [1, Xs],
+                     "relaxation_parameters": [0.0, 1 / (0.5 + sigma0)], "equilibrium": [U, U**2 / 2]}],
+        "init": {U: (_bump, (-1.0, 1.0, 1))},
+        "boundary_conditions": {0: {"method": {0: bc.Neumann}}},
+        "generator": generator,
+        "parameters": {la_c: 1.0, sigma0: 1 / 1.8 - 0.5},
+    }
+
+
+def advection_reaction_1d(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Advection with a logistic reaction source mu u (1 - u), D1Q2
+    (demo/1D/advection_reaction.py:50-105)."""
+    Xs, U = sp.symbols("X, u")
+    C, MU, la_c = sp.symbols("c, mu, lambda", constants=True)
+
+    def u_init(x, xmin, xmax):
+        middle, width = 0.5 * (xmin + xmax), 0.1 * (xmax - xmin)
+        xc = xmin + x % (xmax - xmin)
+        return 0.25 + 0.125 / width**10 * (xc - middle - width)**5 * (middle - xc - width)**5 * (
+            abs(xc - middle) <= width)
+
+    return {
+        "box": {"x": [0.0, 1.0], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [{"velocities": [1, 2], "conserved_moments": U, "polynomials": [1, Xs],
+                     "relaxation_parameters": [0.0, 2.0], "equilibrium": [U, C * U],
+                     "source_terms": {U: MU * U * (1 - U)}}],
+        "init": {U: (u_init, (0.0, 1.0))},
+        "generator": generator,
+        "parameters": {la_c: 1.0, C: 0.25, MU: 1.0},
+    }
+
+
+def shallow_water(dx=1.0 / 64, bc=None, generator="cuda"):
+    """Shallow water, three D2Q4 with relative velocity q/h (demo/2D/shallow_water.py:36-115).
+
+    Periodic [-1, 1]^2, la = 4, g = 1, a raised disc of water.
+    """
+    H, QXs, QYs = sp.symbols("h, qx, qy")
+    la_c, G = sp.symbols("lambda, g", constants=True)
+    s_hx, s_hxy, s_qx, s_qxy = sp.symbols("sigma_0, sigma_1, sigma_2, sigma_3", constants=True)
+    xmin, xmax, ymin, ymax = -1.0, 1.0, -1.0, 1.0
+    rate_hx, rate_hxy = 1 / (0.5 + s_hx), 1 / (0.5 + s_hxy)
+    rate_qx, rate_qxy = 1 / (0.5 + s_qx), 1 / (0.5 + s_qxy)
+    vel, polys = list(range(1, 5)), [1, X, Y, X**2 - Y**2]
+
+    def h_init(x, y, xmin, xmax, ymin, ymax):
+        center = (0.5 * xmin + 0.5 * xmax, 0.5 * ymin + 0.5 * ymax)
+        return 1 + 0.5 * ((x - center[0])**2 + (y - center[1])**2 < 0.1**2)
+
+    return {
+        "parameters": {la_c: 4, G: 1.0, s_hx: 1.0e-3, s_hxy: 0.5, s_qx: 1.0e-1, s_qxy: 0.5},
+        "box": {"x": [xmin, xmax], "y": [ymin, ymax], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [
+            {"velocities": vel, "conserved_moments": H, "polynomials": polys,
+             "relaxation_parameters": [0.0, rate_hx, rate_hx, rate_hxy], "equilibrium": [H, QXs, QYs, 0.0]},
+            {"velocities": vel, "conserved_moments": QXs, "polynomials": polys,
+             "relaxation_parameters": [0.0, rate_qx, rate_qx, rate_qxy],
+             "equilibrium": [QXs, QXs**2 / H + G * H**2 / 2, QXs * QYs / H, 0.0]},
+            {"velocities": vel, "conserved_moments": QYs, "polynomials": polys,
+             "relaxation_parameters": [0.0, rate_qx, rate_qx, rate_qxy],
+             "equilibrium": [QYs, QXs * QYs / H, QYs**2 / H + G * H**2 / 2, 0.0]},
+        ],
+        "init": {H: (h_init, (xmin, xmax, ymin, ymax)), QXs: 0.0, QYs: 0.0},
+        "relative_velocity": [QXs / H, QYs / H],
+        "generator": generator,
+    }
+
+
 # name: (dictionary builder, final time, golden file, {golden field: conserved moment name})
 CASES = {
     "poiseuille": (poiseuille, 0.5, "test2D_poiseuille", {"rho": "rho", "qx": "qx", "qy": "qy"}),
@@ -634,6 +754,135 @@ CASES = {
                          {"rho": "rho", "qx": "qx", "qy": "qy", "T": "T"}),
     "rayleigh_benard": (rayleigh_benard, 0.5, "test2D_rayleigh_benard",
                         {"rho": "rho", "qx": "qx", "qy": "qy", "T": "T"}),
+    "advection_1d": (advection_1d, 0.5, "test1D_advection", {"u": "u"}),
+    "burgers_1d": (burgers_1d, 0.5, "test1D_burgers", {"u": "u"}),
+    "advection_reaction_1d": (advection_reaction_1d, 0.5, "test1D_advection_reaction", {"u": "u"}),
+    "shallow_water": (shallow_water, 0.5, "test2D_shallow_water", {"h": "h", "qx": "qx", "qy": "qy"}),
     "euler_1d": (euler_1d, 0.5, "test1D_euler", {"rho": "rho", "q": "q", "E": "E"}),
     "poiseuille_3d": (poiseuille_3d, 0.5, "test3D_poseuille", {"p": "p", "ux": "ux", "uy": "uy", "uz": "uz"}),
 }
+
+
+def advection_init_f(dx=1.0 / 64, bc=None, generator="cuda"):
+    """2D advection initialised by its distributions (demo/2D/advection_init_f.py:25-105)."""
+    d = advection_2d(dx=dx, bc=bc, generator=generator)
+    cx, cy, la = 0.2, 0.5, 2.0
+    xmin, xmax, ymin, ymax = 0.0, 1.0, 0.0, 1.0
+
+    def u_init(x, y, xmin, xmax, ymin, ymax):
+        center = (0.75 * xmin + 0.25 * xmax, 0.50 * ymin + 0.50 * ymax)
+        return 1 + (1.5 - 1) * ((x - center[0])**2 + (y - center[1])**2 < 0.1**2)
+
+    def f_init(x, y, k, cx, cy, xmin, xmax, ymin, ymax):
+        coeff = 0.25 + 0.5 * (cx, cy, -cx, -cy)[k]
+        return coeff * u_init(x, y, xmin, xmax, ymin, ymax)
+
+    d["inittype"] = "distributions"
+    d["init"] = {k: (f_init, (k, cx / la, cy / la, xmin, xmax, ymin, ymax)) for k in range(4)}
+    return d
+
+
+CASES["advection_init_f"] = (advection_init_f, 0.5, "test2D_advection_init_f", {"U": "U"})
+
+
+# ---------------------------------------------------------------------------
+# 1D Riemann problems (demo/1D/riemann_problems/*.py): D1Q2 per conserved
+# quantity, symbolic rates 1/(1/2 + sigma), Neumann ends, piecewise-constant
+# initial state (riemann_pb of exact_solvers/riemann_solvers.py:21-48).
+
+def _riemann(x, xmid, left, right):
+    out = np.empty(x.shape)
+    out[x < xmid] = left
+    out[x >= xmid] = right
+    return out
+
+
+def _riemann_system(xmin, xmax, la, fields, rates, flux, states, params, dx, bc, generator):
+    """fields: conserved symbols; rates: sigma symbol -> s; flux: equilibrium
+    of the first-order moment of each field; states: (left, right) per field."""
+    bc = _bc(bc)
+    Xs = sp.Symbol("X")
+    la_c = sp.symbols("lambda", constants=True)
+    xmid = 0.5 * (xmin + xmax)
+    schemes = [{"velocities": [1, 2], "conserved_moments": f, "polynomials": [1, Xs],
+                "relaxation_parameters": [0, 1 / (0.5 + sig)], "equilibrium": [f, fl]}
+               for f, sig, fl in zip(fields, rates, flux)]
+    prm = {la_c: la}
+    prm.update({sig: 1 / s - 0.5 for sig, s in rates.items()})
+    prm.update(params)
+    return {
+        "box": {"x": [xmin, xmax], "label": 0},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": schemes,
+        "init": {f: (_riemann, (xmid, l, r)) for f, (l, r) in zip(fields, states)},
+        "boundary_conditions": {0: {"method": {i: bc.Neumann for i in range(len(fields))}}},
+        "generator": generator,
+        "parameters": prm,
+    }
+
+
+def riemann_advection(dx=1.0 / 64, bc=None, generator="cuda"):
+    """demo/1D/riemann_problems/advection.py:24-82: u_t + c u_x = 0, c = 1/4, s = 1.9."""
+    U = sp.Symbol("u")
+    C, SIG = sp.symbols("c, sigma", constants=True)
+    return _riemann_system(0.0, 1.0, 1.0, [U], {SIG: 1.9}, [C * U], [(1.0, 0.0)], {C: 0.25}, dx, bc, generator) | {
+        "init": {U: (_riemann, (0.25, 1.0, 0.0))}}
+
+
+def riemann_burgers(dx=1.0 / 64, bc=None, generator="cuda"):
+    """demo/1D/riemann_problems/burgers.py:28-81: rarefaction 0 | 0.3 on [-1, 1], s = 1.8."""
+    U = sp.Symbol("u")
+    SIG = sp.Symbol("sigma", constants=True)
+    return _riemann_system(-1.0, 1.0, 1.0, [U], {SIG: 1.8}, [U**2 / 2], [(0.0, 0.3)], {}, dx, bc, generator)
+
+
+def riemann_euler(dx=1.0 / 64, bc=None, generator="cuda"):
+    """demo/1D/riemann_problems/euler.py:38-121: Sod tube, gamma = 1.4, la = 3."""
+    RHOs, Q, E = sp.symbols("rho, q, E")
+    GAMMA = sp.Symbol("gamma", constants=True)
+    s1, s2, s3 = sp.symbols("sigma_1, sigma_2, sigma_3", constants=True)
+    gamma = 1.4
+    flux = [Q, (GAMMA - 1) * E + (3 - GAMMA) / 2 * Q**2 / RHOs,
+            GAMMA * E * Q / RHOs - (GAMMA - 1) / 2 * Q**3 / RHOs**2]
+    states = [(1, 1 / 8), (0, 0), (1 / (gamma - 1.0), 0.1 / (gamma - 1.0))]
+    return _riemann_system(0.0, 1.0, 3.0, [RHOs, Q, E], {s1: 1.9, s2: 1.5, s3: 1.4}, flux, states,
+                           {GAMMA: gamma}, dx, bc, generator)
+
+
+def riemann_euler_isothermal(dx=1.0 / 64, bc=None, generator="cuda"):
+    """demo/1D/riemann_problems/euler_isothermal.py:40-109: c0 = la / sqrt(3), rho 2/3 | 4/3."""
+    RHOs, Q = sp.symbols("rho, q")
+    CO = sp.Symbol("c_0", constants=True)
+    s1, s2 = sp.symbols("sigma_1, sigma_2", constants=True)
+    return _riemann_system(-1, 1, 1.0, [RHOs, Q], {s1: 2.0, s2: 1.85}, [Q, Q**2 / RHOs + CO**2 * RHOs],
+                           [(1 - 1 / 3, 1 + 1 / 3), (0, 0)], {CO: 1.0 / np.sqrt(3)}, dx, bc, generator)
+
+
+def riemann_p_system(dx=1.0 / 64, bc=None, generator="cuda"):
+    """demo/1D/riemann_problems/p_system.py:28-95: p(u) = u^-gamma, gamma = 2/3, la = 2."""
+    U1, U2 = sp.symbols("u_1, u_2")
+    GAMMA = sp.Symbol("gamma", constants=True)
+    s1, s2 = sp.symbols("sigma_1, sigma_2", constants=True)
+    return _riemann_system(0.0, 1.0, 2.0, [U1, U2], {s1: 1.9, s2: 1.9}, [-U2, U1**(-GAMMA)],
+                           [(1.50, 0.50), (1.25, 1.50)], {GAMMA: 2.0 / 3.0}, dx, bc, generator)
+
+
+def riemann_shallow_water(dx=1.0 / 64, bc=None, generator="cuda"):
+    """demo/1D/riemann_problems/shallow_water.py:27-92: dam break h 2 | 1, q 0.1 | 0, g = 1, la = 2."""
+    H, Q = sp.symbols("h, q")
+    G = sp.Symbol("g", constants=True)
+    s1, s2 = sp.symbols("sigma_1, sigma_2", constants=True)
+    return _riemann_system(-1, 1.0, 2.0, [H, Q], {s1: 1.5, s2: 1.5}, [Q, Q**2 / H + 0.5 * G * H**2],
+                           [(2, 1), (0.1, 0.0)], {G: 1}, dx, bc, generator)
+
+
+CASES.update({
+    "riemann_advection": (riemann_advection, 0.5, "test1D_riemann_advection", {"u": "u"}),
+    "riemann_burgers": (riemann_burgers, 0.5, "test1D_riemann_burgers", {"u": "u"}),
+    "riemann_euler": (riemann_euler, 0.5, "test1D_riemann_euler", {"rho": "rho", "q": "q", "E": "E"}),
+    "riemann_euler_isothermal": (riemann_euler_isothermal, 0.5, "test1D_riemann_euler_isothermal",
+                                 {"rho": "rho", "q": "q"}),
+    "riemann_p_system": (riemann_p_system, 0.5, "test1D_riemann_p_system", {"u_1": "u_1", "u_2": "u_2"}),
+    "riemann_shallow_water": (riemann_shallow_water, 0.5, "test1D_riemann_shallow_water", {"h": "h", "q": "q"}),
+})

@@ -68,7 +68,7 @@ def make(name):
         for suffix, part in demo_cases.reduce_field(full[key]).items():
             arrays[key + suffix] = part
     out = os.path.join(HERE, f"demo_{name}.npz")
-    np.savez_compressed(out, mask=mask if mask.size <= 65536 else np.array(bool(mask.all())), steps=np.int64(sim.nt),
+    np.savez_compressed(out, mask=mask if mask.size <= 8192 else np.array(bool(mask.all())), steps=np.int64(sim.nt),
                         final_time=np.float64(final_time), reference_maxdiff=np.float64(worst), **arrays)
     print("wrote", out, sim.nt, "steps")
 

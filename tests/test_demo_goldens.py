@@ -21,7 +21,7 @@ def conserved_fields(sim, moments, fields, mask):
         if mask.ndim:
             v[~mask] = 0.0
         else:
-            assert bool(mask)  # 3D fixtures: every node is fluid
+            assert bool(mask)  # reduced fixtures: every node is fluid
         out[key] = v
     return out
 
