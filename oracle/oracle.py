@@ -148,10 +148,15 @@ class OracleSimulation:
                 m[idx] = val(*coords)
             else:
                 m[idx] = val
-        s, rows, coefs, expos = self._tables()
         if init_type == "moments":
-            lib().oracle_equilibrium(_p(m), self.dim, sc.nv, sc.nconsm, _p(self.n), _p(self.h), len(rows), _p(rows),
-                                     _p(coefs), _p(expos))
+            if self._monomial_equilibrium():
+                s, rows, coefs, expos = self._tables()
+                lib().oracle_equilibrium(_p(m), self.dim, sc.nv, sc.nconsm, _p(self.n), _p(self.h), len(rows),
+                                         _p(rows), _p(coefs), _p(expos))
+            else:  # equilibrium of the whole halo box from the conserved moments (NumPy)
+                cons = m[:sc.nconsm].reshape(sc.nconsm, -1)
+                m = sc.equilibrium_numpy(cons, self.extra_parameters_str()).reshape(m.shape)
+                m = np.ascontiguousarray(m)
             lib().oracle_m2f(_p(m), _p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h), _p(self.invM))
         else:
             self.f[...] = m
@@ -181,7 +186,7 @@ class OracleSimulation:
             rhs = meth.rhs if meth.kind != "neumann" else None
             L.oracle_boundary(_p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h), _p(meth.iload[0]),
                               _p(meth.istore), meth.ncond, _p(rhs) if rhs is not None else None, sign)
-        if sc.Tu is not None or sc.source_terms:
+        if sc.Tu is not None or sc.source_terms or not self._monomial_equilibrium():
             self._frame_step()
         else:
             s, rows, coefs, expos = self._tables()
@@ -195,6 +200,17 @@ class OracleSimulation:
     def run(self, nsteps):
         for _ in range(int(nsteps)):
             self.one_time_step()
+
+    def _monomial_equilibrium(self):
+        """The C step takes the equilibrium as monomials with integer exponents;
+        others (e.g. u^(-2/3) of the p-system) go through the NumPy step."""
+        if not hasattr(self, "_monomial"):
+            try:
+                equilibrium_table(self.scheme, self.extra_parameters_str())
+                self._monomial = True
+            except ValueError:
+                self._monomial = False
+        return self._monomial
 
     # ---------------------------------------------------------------- relative velocity / sources
     def _frame_functions(self):

@@ -97,6 +97,8 @@ class ExprPrinter:
                 return "(LBM_R(1)/(" + "*".join([b] * (-n)) + "))"
             if e.exp == sp.Rational(1, 2):
                 return f"lbm_sqrt({self.p(e.base)})"
+            if e.exp.is_Number:  # real power (e.g. the p-system's u^(-2/3))
+                return f"lbm_pow({self.p(e.base)}, {_lit(to_fraction(e.exp))})"
             raise SchemeError(f"unsupported power {e}")
         raise SchemeError(f"unsupported expression {e} ({type(e).__name__})")
 
@@ -231,7 +233,8 @@ class SchemeSource:
         ref = dict(zip(cons, c0s))
         self.meq_ref = []
         for e in scheme.EQ:
-            v = e.subs(ref)
+            # unshifted storage has no reference state (and c0 = 0 may be singular, e.g. u^(-2/3))
+            v = e.subs(ref) if self.shifted else sp.Integer(0)
             self.meq_ref.append(v)
         if any(v.free_symbols for v in self.meq_ref):
             if self.shifted:
@@ -598,5 +601,6 @@ class SchemeSource:
                 "#include \"lbm_common.cuh\"\n"
                 "using lbm::lbm_fma;\n"
                 "template <typename R> __device__ __forceinline__ R lbm_sqrt(R x) { return sqrt(x); }\n"
+                "template <typename R> __device__ __forceinline__ R lbm_pow(R x, R e) { return pow(x, e); }\n"
                 + self.header() +
                 "#include \"scheme_kernels.cuh\"\n")

@@ -110,6 +110,7 @@ __device__ __forceinline__ F2 operator-(F2 a, F2 b) { return a + (-b); }
 __device__ __forceinline__ F2 operator/(F2 a, F2 b) { return F2(a.v.x / b.v.x, a.v.y / b.v.y); }
 __device__ __forceinline__ F2& operator+=(F2& a, F2 b) { a = a + b; return a; }
 __device__ __forceinline__ F2 sqrt(F2 a) { return F2(sqrtf(a.v.x), sqrtf(a.v.y)); }
+__device__ __forceinline__ F2 pow(F2 a, F2 e) { return F2(powf(a.v.x, e.v.x), powf(a.v.y, e.v.y)); }
 
 // a*b + c with one rounding.  Scheme modules are compiled without implicit
 // contraction, so these are the only fused multiply-adds of the generated

@@ -886,3 +886,46 @@ CASES.update({
     "riemann_p_system": (riemann_p_system, 0.5, "test1D_riemann_p_system", {"u_1": "u_1", "u_2": "u_2"}),
     "riemann_shallow_water": (riemann_shallow_water, 0.5, "test1D_riemann_shallow_water", {"h": "h", "q": "q"}),
 })
+
+
+def bend(dx=1.0 / 64, bc=None, parallelogram=None, generator="cuda"):
+    """Flow around a bend, D2Q9 Geier with relative velocity (demo/2D/bend.py:58-240).
+
+    A solid block fills [0, 0.75]^2 (label 0, Bouzidi bounce-back); parabolic
+    inflow through the left strip (label 2), outflow through the bottom
+    strip (label 1, NeumannY).
+    """
+    bc = _bc(bc)
+    if parallelogram is None:
+        from pylbm_gb300.geometry import Parallelogram as parallelogram
+    la_c = sp.symbols("lambda", constants=True)
+    xmin, xmax, ymin, ymax = 0.0, 1.0, 0.0, 1.0
+    radius, la, rho_o, u_o, mu = 0.25, 1.0, 1.0, 0.05, 2.5e-6
+    zeta = 100 * mu
+    xc, yc = xmax - radius, ymax - radius
+
+    def bc_in(f, m, x, y, rho_o, u_o, ymin, ymax, radius):
+        y_bound = ymax - radius
+        m[RHO] = rho_o
+        m[QX] = rho_o * u_o * 4 * (ymax - y) * (y - y_bound) / (ymax - y_bound)**2
+        m[QY] = 0.0
+
+    return {
+        "box": {"x": [xmin, xmax], "y": [ymin, ymax], "label": [2, 0, 1, 0]},
+        "elements": [parallelogram((xmin, ymin), (xc, ymin), (xmin, yc), label=0)],
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [_geier(la_c, dx, la, rho_o, mu, zeta)],
+        "parameters": {la_c: la},
+        "init": {RHO: rho_o, QX: rho_o * u_o, QY: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack}},
+            1: {"method": {0: bc.NeumannY}},
+            2: {"method": {0: bc.BouzidiBounceBack}, "value": (bc_in, (rho_o, u_o, ymin, ymax, radius))},
+        },
+        "generator": generator,
+        "relative_velocity": [QX / RHO, QY / RHO],
+    }
+
+
+CASES["bend"] = (bend, 0.5, "test2D_coude", {"rho": "rho", "qx": "qx", "qy": "qy"})
