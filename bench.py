@@ -185,8 +185,34 @@ def variants(args):
         out[name] = {"MLUPS": mlups, "ms_per_step": ms / steps, "GB/s": gbs, "hbm_frac": gbs / peak,
                      "steps": steps}
         sim.free()
+    out["tgv3d_256_500_steps_precision"] = tgv_precision()
     out["ensemble_512_d2q9_f16"] = ensemble_variant(peak)
     out["learned_closure_d2q9"] = closure_variant()
+    return out
+
+
+def tgv_precision(n=256, steps=500):
+    """The D3Q19 TGV workload at its full length: relative L2 error of the
+    velocity and of the kinetic-energy density of each storage type against
+    the FP64 run (the form that reproduces pylbm's Cython bit for bit)."""
+    import numpy as np
+    from pylbm_gb300 import Simulation
+    from pylbm_gb300 import workloads as W
+
+    fields = {}
+    for st in ("float64", "float32", "float16", "bfloat16"):
+        sim = Simulation(W.tgv3d(n=n), dtype=st)
+        sim.run(steps)
+        rho = sim.m[W.RHO]
+        u = np.stack([sim.m[q] / rho for q in (W.QX, W.QY, W.QZ)])
+        fields[st] = (u, 0.5 * rho * (u ** 2).sum(axis=0))
+        sim.free()
+    u0, e0 = fields["float64"]
+    out = {"grid": [n, n, n], "steps": steps, "against": "float64"}
+    for st in ("float32", "float16", "bfloat16"):
+        u, e = fields[st]
+        out[st] = {"velocity_rel_l2": float(np.linalg.norm(u - u0) / np.linalg.norm(u0)),
+                   "kinetic_energy_rel_l2": float(np.linalg.norm(e - e0) / np.linalg.norm(e0))}
     return out
 
 

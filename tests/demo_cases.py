@@ -929,3 +929,56 @@ def bend(dx=1.0 / 64, bc=None, parallelogram=None, generator="cuda"):
 
 
 CASES["bend"] = (bend, 0.5, "test2D_coude", {"rho": "rho", "qx": "qx", "qy": "qy"})
+
+
+# ---------------------------------------------------------------------------
+# Stencils reaching two nodes (vmax = 2, two ghost layers).  pylbm has no
+# golden file for them; their fixtures are the reference's own run of the
+# same dictionary (golden file None).
+
+def d1q5_advection(dx=1.0 / 64, bc=None, generator="cuda"):
+    """D1Q5 (velocities 0, +-1, +-2) advection, Neumann ends, Riemann initial state."""
+    bc = _bc(bc)
+    U, Xs = sp.symbols("u, X")
+    la_c, C = sp.symbols("lambda, c", constants=True)
+    return {
+        "box": {"x": [0.0, 1.0], "label": 0},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [{"velocities": list(range(5)), "conserved_moments": U,
+                     "polynomials": [1, Xs, Xs**2 / 2, Xs**3 / 6, Xs**4 / 24],
+                     "relaxation_parameters": [0.0, 1.5, 1.4, 1.3, 1.2],
+                     "equilibrium": [U, C * U, C**2 * U / 2, C**3 * U / 6, C**4 * U / 24]}],
+        "init": {U: (_riemann, (0.3, 1.0, 0.2))},
+        "boundary_conditions": {0: {"method": {0: bc.Neumann}}},
+        "generator": generator,
+        "parameters": {la_c: 2.0, C: 0.25},
+    }
+
+
+def d2q13_advection(dx=1.0 / 32, bc=None, generator="cuda"):
+    """D2Q13 (D2Q9 plus (+-2, 0), (0, +-2)) advection on the torus."""
+    U = sp.Symbol("u")
+    la_c, CX, CY = sp.symbols("lambda, c_x, c_y", constants=True)
+    polys = [1, X, Y, X**2, Y**2, X * Y, X**2 * Y, X * Y**2, X**2 * Y**2, X**3, Y**3, X**4, Y**4]
+    eq = [sp.sympify(p).subs({X: CX, Y: CY}) * U for p in polys]
+
+    def u0(x, y):
+        return 1.0 + 0.5 * ((x - 0.3)**2 + (y - 0.6)**2 < 0.15**2)
+
+    return {
+        "box": {"x": [0.0, 1.0], "y": [0.0, 1.0], "label": -1},
+        "space_step": dx,
+        "scheme_velocity": la_c,
+        "schemes": [{"velocities": list(range(13)), "conserved_moments": U, "polynomials": polys,
+                     "relaxation_parameters": [0.0] + [1.2] * 12, "equilibrium": eq}],
+        "init": {U: u0},
+        "generator": generator,
+        "parameters": {la_c: 2.0, CX: 0.3, CY: -0.2},
+    }
+
+
+CASES.update({
+    "d1q5_advection": (d1q5_advection, 0.5, None, {"u": "u"}),
+    "d2q13_advection": (d2q13_advection, 0.25, None, {"u": "u"}),
+})
