@@ -103,8 +103,18 @@ struct F2 {
   __device__ __forceinline__ explicit F2(int a) { v = make_float2((float)a, (float)a); }
 };
 
-__device__ __forceinline__ F2 operator+(F2 a, F2 b) { F2 r; r.v = __fadd2_rn(a.v, b.v); return r; }
-__device__ __forceinline__ F2 operator*(F2 a, F2 b) { F2 r; r.v = __fmul2_rn(a.v, b.v); return r; }
+// The packed operations are written as PTX with an explicit rounding mode:
+// ptxas never contracts .rn-qualified instructions, so a packed multiply
+// followed by a packed add stays two roundings, exactly as the scalar code
+// of a module built with -fmad=false.
+#define LBM_F2_OP2(OP)                                                                          \
+  asm("{\n\t.reg .b64 A, B, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t" OP            \
+      " D, A, B;\n\tmov.b64 {%0, %1}, D;\n\t}"                                                  \
+      : "=f"(r.v.x), "=f"(r.v.y)                                                                \
+      : "f"(a.v.x), "f"(a.v.y), "f"(b.v.x), "f"(b.v.y))
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { F2 r; LBM_F2_OP2("add.rn.f32x2"); return r; }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { F2 r; LBM_F2_OP2("mul.rn.f32x2"); return r; }
+#undef LBM_F2_OP2
 __device__ __forceinline__ F2 operator-(F2 a) { return F2(-a.v.x, -a.v.y); }
 __device__ __forceinline__ F2 operator-(F2 a, F2 b) { return a + (-b); }
 __device__ __forceinline__ F2 operator/(F2 a, F2 b) { return F2(a.v.x / b.v.x, a.v.y / b.v.y); }
@@ -123,7 +133,14 @@ __device__ __forceinline__ double lbm_fma<double>(double a, double b, double c) 
 template <>
 __device__ __forceinline__ float lbm_fma<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 template <>
-__device__ __forceinline__ F2 lbm_fma<F2>(F2 a, F2 b, F2 c) { F2 r; r.v = __ffma2_rn(a.v, b.v, c.v); return r; }
+__device__ __forceinline__ F2 lbm_fma<F2>(F2 a, F2 b, F2 c) {
+  F2 r;
+  asm("{\n\t.reg .b64 A, B, C, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\tmov.b64 C, {%6, %7};\n\t"
+      "fma.rn.f32x2 D, A, B, C;\n\tmov.b64 {%0, %1}, D;\n\t}"
+      : "=f"(r.v.x), "=f"(r.v.y)
+      : "f"(a.v.x), "f"(a.v.y), "f"(b.v.x), "f"(b.v.y), "f"(c.v.x), "f"(c.v.y));
+  return r;
+}
 
 // ---------------------------------------------------------------- geometry
 // Kernel-side copy of lbm_lattice (without the shift table).

@@ -447,10 +447,38 @@ class Simulation:
                                                      ctypes.byref(self._mlat), self._stream))
             self._update_m = False
         if idx not in self._m_cache:
-            plane = np.empty(self._mlat.vstride, dtype=np.float64)
-            self._mbuf().download(plane, offset=idx * self._mlat.vstride * 8, stream=self._stream)
-            self._m_cache[idx] = np.array(self._plane_view(plane, self._mlat))
+            # the conserved moments (what users and writers read) come in one
+            # device-to-host copy; other moments one plane at a time
+            first, count = (0, self.scheme.nconsm) if idx < self.scheme.nconsm else (idx, 1)
+            planes = np.empty(count * self._mlat.vstride, dtype=np.float64)
+            self._mbuf().download(planes, offset=first * self._mlat.vstride * 8, stream=self._stream)
+            for j in range(count):
+                if first + j not in self._m_cache:
+                    plane = planes[j * self._mlat.vstride:(j + 1) * self._mlat.vstride]
+                    self._m_cache[first + j] = np.array(self._plane_view(plane, self._mlat))
         return self._m_cache[idx]
+
+    def fields(self):
+        """Conserved moments on the interior, {name: array}, read with one device-to-host copy."""
+        return {str(c): self.m[c] for c in self.scheme.consm}
+
+    def write_h5(self, filename, path="", timestep=None, vectors=None):
+        """Write the conserved moments (and {name: [moment names]} vectors) as
+        HDF5 + XDMF (pylbm/hdf5.py H5File, as used by the demos' ``save``)."""
+        from .output import H5File
+
+        h5 = H5File(None, filename, path, timestep)
+        h5.set_grid(*self.domain.coords)
+        fields = self.fields()
+        used = set()
+        for name, comps in (vectors or {}).items():
+            h5.add_vector(name, [fields[c] for c in comps])
+            used.update(comps)
+        for name, arr in fields.items():
+            if name not in used:
+                h5.add_scalar(name, arr)
+        h5.save()
+        return h5
 
     def _inner(self):
         return tuple(slice(int(h), -int(h)) for h in self.domain.halo)

@@ -31,3 +31,26 @@ def test_cuda_reproduces_reference_golden(name):
     demo_cases.run_to(o, final_time)
     assert rel_err(m, o.moments()).max() < 1e-10
     sim.free()
+
+
+def test_h5_output_matches_reference_golden_file(tmp_path):
+    """sim.write_h5 (one device-to-host copy of the conserved moments) gives
+    the fields of pylbm's own golden HDF5 file for the Poiseuille demo."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import h5lite
+
+    build, final_time, _, fields = demo_cases.CASES["poiseuille"]
+    g = golden("demo_poiseuille.npz")
+    sim = Simulation(build())
+    demo_cases.run_to(sim, final_time)
+    sim.write_h5("poiseuille", str(tmp_path))
+    back = h5lite.read(str(tmp_path / "poiseuille.h5"))
+    assert np.array_equal(back["x_0"], sim.domain.coords[0]) and np.array_equal(back["x_1"], sim.domain.coords[1])
+    for key, cons in fields.items():
+        ref = g[key]
+        diff = np.abs(back[cons].T - ref)
+        assert np.all(diff <= np.maximum(1e-14 * np.abs(ref), 1e-7)), key
+    assert (tmp_path / "poiseuille.xdmf").exists()
+    sim.free()
