@@ -174,6 +174,9 @@ def variants(args):
         ("tgv3d_256_bf16", lambda: Simulation(W.tgv3d(n=256), dtype="bfloat16"), 256 ** 3, 19, 2, 100),
         ("cavity_256_f64_parity", lambda: Simulation(W.cavity(n=256)), 256 ** 2, 9, 8, 1000),
         ("cylinder_2048x512_f32", lambda: Simulation(W.cylinder(), dtype="float32"), 2048 * 512, 9, 4, 1000),
+        # relative-velocity (Geier) collide, Bouzidi walls and disc, NeumannX outflow
+        ("karman_geier_2048x1024_f32", lambda: Simulation(W.karman(dx=1.0 / 1024), dtype="float32"),
+         2048 * 1024, 9, 4, 500),
     ]
     for name, make, nodes, q, es, steps in cases:
         sim = make()

@@ -165,6 +165,75 @@ int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* 
                                  int32_t ncond, const double* rhs, const double* dist, const lbm_lattice* lat,
                                  int32_t ordered, void* stream);
 
+/* ------------------------------------------------------------------ */
+/* Domain construction on the device (pylbm/domain.py:87-620 and the  */
+/* link lists of pylbm/boundary.py:23-160): fluid/solid map, per-link */
+/* wall distance and label, and the boundary links they define.  The   */
+/* arrays cover the halo-extended box, last axis contiguous, no        */
+/* padding; for each unique velocity u of the stencil,                 */
+/* distance[u][node] is the fraction of the link node -> node + v_u    */
+/* before a wall (999 where none) and flag[u][node] that wall's label  */
+/* (999 where none); in_or_out is 999 in the fluid, -1 elsewhere.      */
+/* Arithmetic follows the host rules operation by operation (IEEE,     */
+/* no fused multiply-adds), so the arrays equal the host ones bit for  */
+/* bit.                                                                */
+/* ------------------------------------------------------------------ */
+
+typedef struct lbm_domain {
+  int32_t dim;                /* 1, 2 or 3 */
+  int32_t nu;                 /* unique velocities */
+  int32_t n[3];               /* halo-extended nodes per axis (1 beyond dim) */
+  int32_t halo[3];            /* ghost layers per axis */
+  int32_t vel[LBM_MAX_Q][3];  /* unique velocities */
+  double dx;                  /* space step */
+} lbm_domain;
+
+#define LBM_ELEMENT_CIRCLE 1        /* p = cx, cy, radius; one label */
+#define LBM_ELEMENT_PARALLELOGRAM 2 /* p = point x, y, v1 x, y, v2 x, y; labels of the 4 edges */
+
+typedef struct lbm_element {
+  int32_t kind;
+  int32_t isfluid;            /* 1: the element carves fluid out of solid */
+  int32_t label[4];
+  double p[8];
+  int32_t lo[3], hi[3];       /* halo-coordinate region [lo, hi) the element touches */
+} lbm_element;
+
+/* in_or_out = -1 with 999 on the interior, distance = 999, flag = 999
+ * (pylbm/domain.py:87-160). */
+int lbm_domain_reset(const lbm_domain* d, double* in_or_out, double* distance, int32_t* flag, void* stream);
+
+/* Box walls: for every axis and every unique velocity leaving the box
+ * through a side whose label is not -2, the first |v| interior layers get
+ * distance (i + 1/2)/|v| and that side's label where this is shorter than
+ * the current distance (pylbm/domain.py:463-521). */
+int lbm_domain_box(const lbm_domain* d, const int32_t* box_label, double* distance, int32_t* flag, void* stream);
+
+/* One obstacle (pylbm/domain.py:523-620): nodes of the element become solid
+ * (fluid for isfluid elements), then each fluid node of the region whose
+ * link v_u ends in a solid node and crosses the element's boundary within
+ * one link gets the crossing fraction and edge label (shortest wins).
+ * `coords` holds the halo coordinates of axis 0, then 1, then 2. */
+int lbm_domain_element(const lbm_domain* d, const lbm_element* e, const double* coords, double* in_or_out,
+                       double* distance, int32_t* flag, void* stream);
+
+/* Links starting in solid nodes are removed (pylbm/domain.py ``clean``). */
+int lbm_domain_clean(const lbm_domain* d, const double* in_or_out, double* distance, int32_t* flag,
+                     void* stream);
+
+/* Boundary links of one label and one unique velocity u, in row-major node
+ * order (np.where of pylbm/boundary.py:23-47): every node with
+ * flag[u][node] == label gives the row node + vsym (its halo coordinates)
+ * and distance[u][node].  Two passes: lbm_links_count writes the count of
+ * each block of lbm_links_block() nodes (blocks = ceil(nodes / block));
+ * the caller prefix-sums them into offsets and lbm_links_fill writes rows
+ * (count, dim) int32 and distances (count) float64. */
+int32_t lbm_links_block(void);
+int lbm_links_count(const lbm_domain* d, const int32_t* flag, int32_t u, int32_t label, int32_t* block_counts,
+                    void* stream);
+int lbm_links_fill(const lbm_domain* d, const int32_t* flag, const double* distance, int32_t u, int32_t label,
+                   const int32_t* vsym, const int32_t* block_offsets, int32_t* rows, double* dist, void* stream);
+
 /* Block average of the interior populations over factor^dim nodes into a
  * dense float64 array out[nv][n0/factor][n1/factor][n2/factor] (physical
  * values, last axis contiguous): restriction of a fine run onto a coarse

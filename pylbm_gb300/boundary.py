@@ -27,6 +27,9 @@ class _BoundaryVelocity:
         from .stencil import velocity_number
         num = velocity_number(tuple(int(c) for c in vsym))
         ksym_u = int(st.unum2index[num])
+        if getattr(domain, "device", False):  # flags on the GPU: extracted there, same order
+            self.indices, self.distance = domain.link_list(label, ksym_u, vsym)
+            return
         ind = np.where(domain.flag[ksym_u] == label)
         self.indices = np.array(ind, dtype=np.int64)
         if self.indices.size:

@@ -1,0 +1,401 @@
+// Domain construction on the device: fluid/solid map, per-link wall
+// distances and labels, and the boundary links they define.
+//
+// Same rules as the host Domain/Boundary (pylbm/domain.py:87-620,
+// pylbm/boundary.py:23-160); every floating-point operation is written
+// with an explicit IEEE intrinsic (no contraction) in the order the host
+// evaluates it, so both give identical arrays.
+#include "lbm_common.cuh"
+
+using namespace lbm;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr double kValIn = 999.0;
+constexpr double kValOut = -1.0;
+constexpr double kFar = 1.0e16;  // "no intersection" of the element distance rules
+
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+struct Box {
+  int dim, nu;
+  int n[3];
+  long long stride[3];
+  long long nodes;
+};
+
+inline Box make_box(const lbm_domain& d) {
+  Box b;
+  b.dim = d.dim;
+  b.nu = d.nu;
+  for (int k = 0; k < 3; ++k) b.n[k] = k < d.dim ? d.n[k] : 1;
+  b.stride[2] = 1;
+  b.stride[1] = b.n[2];
+  b.stride[0] = (long long)b.n[1] * b.n[2];
+  b.nodes = (long long)b.n[0] * b.n[1] * b.n[2];
+  return b;
+}
+
+// node -> (i0, i1, i2) of the (up to) 3D box; unused axes have n = 1
+__device__ __forceinline__ void unflatten(const Box& b, long long node, int (&i)[3]) {
+  i[2] = (int)(node % b.n[2]);
+  long long r = node / b.n[2];
+  i[1] = (int)(r % b.n[1]);
+  i[0] = (int)(r / b.n[1]);
+}
+
+// ------------------------------------------------------------------ reset
+__global__ void k_reset(Box b, lbm_domain d, double* ioo, double* dist, int* flag) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.nodes) return;
+  int i[3];
+  unflatten(b, t, i);
+  bool inner = true;
+  for (int a = 0; a < b.dim; ++a) inner = inner && i[a] >= d.halo[a] && i[a] < b.n[a] - d.halo[a];
+  ioo[t] = inner ? kValIn : kValOut;
+  for (int u = 0; u < b.nu; ++u) {
+    dist[u * b.nodes + t] = kValIn;
+    flag[u * b.nodes + t] = 999;
+  }
+}
+
+// ------------------------------------------------------------------ box walls
+struct BoxLabels {
+  int label[6];
+};
+
+// one thread per (u, node): the candidates of the axes in order, strict "shorter" rule
+__global__ void k_box(Box b, lbm_domain d, BoxLabels L, double* dist, int* flag) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.nodes * b.nu) return;
+  const int u = (int)(t / b.nodes);
+  const long long node = t - (long long)u * b.nodes;
+  int i[3];
+  unflatten(b, node, i);
+  for (int a = 0; a < b.dim; ++a)
+    if (i[a] < d.halo[a] || i[a] >= b.n[a] - d.halo[a]) return;  // interior nodes only
+  double dv = dist[t];
+  int fv = flag[t];
+  for (int a = 0; a < b.dim; ++a) {
+    const int c = d.vel[u][a];
+    const int nin = b.n[a] - 2 * d.halo[a];
+    const int ia = i[a] - d.halo[a];
+    if (c < 0 && L.label[2 * a] != -2) {
+      if (ia < -c) {
+        const double dd = dvd(add((double)ia, 0.5), (double)(-c));
+        if (dv > dd) {
+          dv = dd;
+          fv = L.label[2 * a];
+        }
+      }
+    } else if (c > 0 && L.label[2 * a + 1] != -2) {
+      const int from_end = nin - 1 - ia;
+      if (from_end < c) {
+        const double dd = dvd(add((double)from_end, 0.5), (double)c);
+        if (dv > dd) {
+          dv = dd;
+          fv = L.label[2 * a + 1];
+        }
+      }
+    }
+  }
+  dist[t] = dv;
+  flag[t] = fv;
+}
+
+// ------------------------------------------------------------------ elements
+struct Region {
+  int lo[3], hi[3];
+  long long nodes;
+};
+
+__device__ __forceinline__ void region_node(const Region& r, long long t, int (&i)[3]) {
+  const int n1 = r.hi[1] - r.lo[1], n2 = r.hi[2] - r.lo[2];
+  i[2] = r.lo[2] + (int)(t % n2);
+  const long long q = t / n2;
+  i[1] = r.lo[1] + (int)(q % n1);
+  i[0] = r.lo[0] + (int)(q / n1);
+}
+
+__device__ __forceinline__ bool inside(const lbm_element& e, double x, double y) {
+  if (e.kind == LBM_ELEMENT_CIRCLE) {
+    const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
+    return add(mul(px, px), mul(py, py)) <= mul(e.p[2], e.p[2]);
+  }
+  // parallelogram: barycentric coordinates in (v1, v2)
+  const double dx = sub(x, e.p[0]), dy = sub(y, e.p[1]);
+  const double inv = dvd(1.0, sub(mul(e.p[2], e.p[5]), mul(e.p[3], e.p[4])));
+  const double a = mul(sub(mul(dx, e.p[5]), mul(dy, e.p[4])), inv);
+  const double bb = mul(sub(mul(dy, e.p[2]), mul(dx, e.p[3])), inv);
+  return a >= 0 && bb >= 0 && a <= 1 && bb <= 1;
+}
+
+// first crossing of the ray (x, y) + t v, t in (0, dmax], with the element
+// boundary: t (or -1) and the label of the crossed edge (or -1)
+__device__ __forceinline__ double crossing(const lbm_element& e, double x, double y, double vx, double vy,
+                                          double dmax, int& border) {
+  border = -1;
+  if (e.kind == LBM_ELEMENT_CIRCLE) {
+    // ellipse {c + cos(a) v1 + sin(a) v2} with v1 = (r, 0), v2 = (0, r)
+    const double r = e.p[2];
+    const double v1x = mul(r, 1.0), v1y = mul(r, 0.0), v2x = mul(r, 0.0), v2y = mul(r, 1.0);
+    const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
+    const double sxx = add(mul(v1x, v1x), mul(v2x, v2x));
+    const double syy = add(mul(v1y, v1y), mul(v2y, v2y));
+    const double sxy = mul(2.0, add(mul(v1x, v1y), mul(v2x, v2y)));
+    const double det = sub(mul(v1x, v2y), mul(v1y, v2x));
+    const double det2 = mul(det, det);
+    const double qa = sub(add(mul(mul(vx, vx), syy), mul(mul(vy, vy), sxx)), mul(mul(vx, vy), sxy));
+    const double qb = sub(add(mul(mul(mul(2.0, px), vx), syy), mul(mul(mul(2.0, py), vy), sxx)),
+                          mul(add(mul(px, vy), mul(py, vx)), sxy));
+    const double qc = sub(sub(add(mul(mul(px, px), syy), mul(mul(py, py), sxx)), mul(mul(px, py), sxy)), det2);
+    const double disc = sub(mul(qb, qb), mul(mul(4.0, qa), qc));
+    const bool ok = disc >= 0;
+    const double root = __dsqrt_rn(ok ? disc : 0.0);
+    double t1 = kFar, t2 = kFar;
+    if (qa != 0) {
+      t1 = ok ? dvd(sub(-qb, root), mul(2.0, qa)) : kFar;
+      t2 = ok ? dvd(add(-qb, root), mul(2.0, qa)) : kFar;
+    }
+    if (t1 < 0) t1 = kFar;
+    if (t2 < 0) t2 = kFar;
+    double t = ok ? fmin(t1, t2) : -1.0;
+    if (t == kFar) t = -1.0;
+    if (t > 0 && t <= dmax) {
+      border = e.label[0];
+      return t;
+    }
+    return -1.0;
+  }
+  // parallelogram: the four edges point + s w, s in [0, 1], in the host order
+  const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
+  const double q[4][2] = {{0.0, 0.0}, {0.0, 0.0}, {e.p[4], e.p[5]}, {e.p[2], e.p[3]}};
+  const double w[4][2] = {{e.p[2], e.p[3]}, {e.p[4], e.p[5]}, {e.p[2], e.p[3]}, {e.p[4], e.p[5]}};
+  double alpha = kFar;
+  for (int k = 0; k < 4; ++k) {
+    const double det = sub(mul(vy, w[k][0]), mul(vx, w[k][1]));
+    if (det == 0) continue;
+    const double inv = dvd(1.0, det);
+    const double c1 = sub(q[k][0], px), c2 = sub(q[k][1], py);
+    const double t = mul(add(mul(-w[k][1], c1), mul(w[k][0], c2)), inv);
+    const double s = mul(add(mul(-vy, c1), mul(vx, c2)), inv);
+    if (t > 0 && s >= 0 && s <= 1 && t <= dmax && alpha > t) {
+      alpha = t;
+      border = e.label[k];
+    }
+  }
+  if (alpha == kFar) {
+    border = -1;
+    return -1.0;
+  }
+  return alpha;
+}
+
+__device__ __forceinline__ long long box_offset(const Box& b, const int (&i)[3]) {
+  return (long long)i[0] * b.stride[0] + (long long)i[1] * b.stride[1] + i[2];
+}
+
+__global__ void k_element_map(Box b, Region r, lbm_element e, const double* __restrict__ c0,
+                              const double* __restrict__ c1, double* ioo) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= r.nodes) return;
+  int i[3];
+  region_node(r, t, i);
+  const bool in = inside(e, c0[i[0]], c1[i[1]]);
+  if (in) ioo[box_offset(b, i)] = e.isfluid ? kValIn : kValOut;
+}
+
+__global__ void k_element_links(Box b, lbm_domain d, Region r, lbm_element e, const double* __restrict__ c0,
+                                const double* __restrict__ c1, const double* __restrict__ ioo, double* dist,
+                                int* flag) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= r.nodes * b.nu) return;
+  const int u = (int)(t / r.nodes);
+  const int vx = d.vel[u][0], vy = d.vel[u][1], vz = d.vel[u][2];
+  if (vx == 0 && vy == 0 && vz == 0) return;
+  int i[3];
+  region_node(r, t - (long long)u * r.nodes, i);
+  const double x = c0[i[0]], y = c1[i[1]];
+  const bool in = inside(e, x, y);
+  const bool solid = e.isfluid ? !in : in;
+  const long long o = box_offset(b, i);
+  int j[3] = {i[0] + vx, i[1] + vy, i[2] + vz};
+  const bool out = ioo[box_offset(b, j)] == kValOut;
+  int border;
+  const double alpha = crossing(e, x, y, mul(d.dx, (double)vx), mul(d.dx, (double)vy), 1.0, border);
+  const bool sel = alpha > 0 && !solid && out;
+  double dk = dist[(long long)u * b.nodes + o];
+  int fk = flag[(long long)u * b.nodes + o];
+  if (e.isfluid) {
+    if (!out && ioo[o] == kValIn) {
+      dk = kValIn;
+      fk = 999;
+    }
+  } else if (solid) {
+    dk = kValIn;
+    fk = 999;
+  }
+  const bool keep = e.isfluid ? (alpha > dk || dk == kValIn) : (alpha < dk);
+  if (sel && keep) {
+    dk = alpha;
+    fk = border;
+  }
+  dist[(long long)u * b.nodes + o] = dk;
+  flag[(long long)u * b.nodes + o] = fk;
+}
+
+__global__ void k_clean(Box b, const double* __restrict__ ioo, double* dist, int* flag) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.nodes * b.nu) return;
+  const long long node = t % b.nodes;
+  if (ioo[node] == kValOut && dist[t] > 0) {
+    dist[t] = kValIn;
+    flag[t] = 999;
+  }
+}
+
+// ------------------------------------------------------------------ link lists
+__global__ void __launch_bounds__(kThreads) k_links_count(Box b, const int* __restrict__ flag, int u, int label,
+                                                          int* counts) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool hit = t < b.nodes && flag[(long long)u * b.nodes + t] == label;
+  const int c = __syncthreads_count(hit);
+  if (threadIdx.x == 0) counts[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(kThreads) k_links_fill(Box b, const int* __restrict__ flag,
+                                                         const double* __restrict__ dist, int u, int label,
+                                                         int3 vsym, const int* __restrict__ offsets, int* rows,
+                                                         double* out_dist) {
+  __shared__ int warp_total[kThreads / 32];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool hit = t < b.nodes && flag[(long long)u * b.nodes + t] == label;
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned ballot = __ballot_sync(0xffffffffu, hit);
+  if (lane == 0) warp_total[warp] = __popc(ballot);
+  __syncthreads();
+  int before = 0;
+  for (unsigned w = 0; w < warp; ++w) before += warp_total[w];
+  if (!hit) return;
+  const int pos = offsets[blockIdx.x] + before + __popc(ballot & ((1u << lane) - 1u));
+  int i[3];
+  unflatten(b, t, i);
+  const int vs[3] = {vsym.x, vsym.y, vsym.z};
+  for (int a = 0; a < b.dim; ++a) rows[(long long)pos * b.dim + a] = i[a] + vs[a];
+  out_dist[pos] = dist[(long long)u * b.nodes + t];
+}
+
+int check_domain(const lbm_domain* d, const char* who) {
+  if (!d) return fail(LBM_ERR_ARG, "%s: NULL domain", who);
+  if (d->dim < 1 || d->dim > 3 || d->nu < 1 || d->nu > LBM_MAX_Q)
+    return fail(LBM_ERR_ARG, "%s: dim=%d nu=%d", who, d->dim, d->nu);
+  for (int a = 0; a < 3; ++a) {
+    if (d->n[a] < 1 || (a >= d->dim && d->n[a] != 1)) return fail(LBM_ERR_ARG, "%s: n[%d]=%d", who, a, d->n[a]);
+    if (a < d->dim && (d->halo[a] < 1 || 2 * d->halo[a] >= d->n[a]))
+      return fail(LBM_ERR_ARG, "%s: halo[%d]=%d for n=%d", who, a, d->halo[a], d->n[a]);
+  }
+  for (int u = 0; u < d->nu; ++u)
+    for (int a = 0; a < 3; ++a) {
+      const int reach = a < d->dim ? d->halo[a] : 0;
+      if (d->vel[u][a] < -reach || d->vel[u][a] > reach)
+        return fail(LBM_ERR_ARG, "%s: velocity %d reaches beyond the halo", who, u);
+    }
+  return LBM_OK;
+}
+
+inline unsigned blocks_for(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+}  // namespace
+
+extern "C" {
+
+int32_t lbm_links_block(void) { return kThreads; }
+
+int lbm_domain_reset(const lbm_domain* d, double* in_or_out, double* distance, int32_t* flag, void* stream) {
+  int rc = check_domain(d, "lbm_domain_reset");
+  if (rc) return rc;
+  if (!in_or_out || !distance || !flag) return fail(LBM_ERR_ARG, "lbm_domain_reset: NULL array");
+  Box b = make_box(*d);
+  k_reset<<<blocks_for(b.nodes), kThreads, 0, (cudaStream_t)stream>>>(b, *d, in_or_out, distance, flag);
+  return launch_check("lbm_domain_reset");
+}
+
+int lbm_domain_box(const lbm_domain* d, const int32_t* box_label, double* distance, int32_t* flag, void* stream) {
+  int rc = check_domain(d, "lbm_domain_box");
+  if (rc) return rc;
+  if (!box_label || !distance || !flag) return fail(LBM_ERR_ARG, "lbm_domain_box: NULL argument");
+  Box b = make_box(*d);
+  BoxLabels L;
+  for (int k = 0; k < 6; ++k) L.label[k] = k < 2 * d->dim ? box_label[k] : -2;
+  k_box<<<blocks_for(b.nodes * b.nu), kThreads, 0, (cudaStream_t)stream>>>(b, *d, L, distance, flag);
+  return launch_check("lbm_domain_box");
+}
+
+int lbm_domain_element(const lbm_domain* d, const lbm_element* e, const double* coords, double* in_or_out,
+                       double* distance, int32_t* flag, void* stream) {
+  int rc = check_domain(d, "lbm_domain_element");
+  if (rc) return rc;
+  if (!e || !coords || !in_or_out || !distance || !flag) return fail(LBM_ERR_ARG, "lbm_domain_element: NULL argument");
+  if (d->dim != 2) return fail(LBM_ERR_UNSUPPORTED, "lbm_domain_element: 2D elements only (dim=%d)", d->dim);
+  if (e->kind != LBM_ELEMENT_CIRCLE && e->kind != LBM_ELEMENT_PARALLELOGRAM)
+    return fail(LBM_ERR_ARG, "lbm_domain_element: kind %d", e->kind);
+  Region r;
+  r.nodes = 1;
+  for (int a = 0; a < 3; ++a) {
+    r.lo[a] = a < d->dim ? e->lo[a] : 0;
+    r.hi[a] = a < d->dim ? e->hi[a] : 1;
+    // the region stays in the interior, so node + v stays in the box
+    if (a < d->dim && (r.lo[a] < d->halo[a] || r.hi[a] > d->n[a] - d->halo[a]))
+      return fail(LBM_ERR_ARG, "lbm_domain_element: region [%d, %d) outside the interior of axis %d", r.lo[a],
+                  r.hi[a], a);
+    if (r.hi[a] <= r.lo[a]) return LBM_OK;
+    r.nodes *= r.hi[a] - r.lo[a];
+  }
+  Box b = make_box(*d);
+  cudaStream_t s = (cudaStream_t)stream;
+  const double* c0 = coords;
+  const double* c1 = coords + d->n[0];
+  k_element_map<<<blocks_for(r.nodes), kThreads, 0, s>>>(b, r, *e, c0, c1, in_or_out);
+  rc = launch_check("lbm_domain_element");
+  if (rc) return rc;
+  k_element_links<<<blocks_for(r.nodes * b.nu), kThreads, 0, s>>>(b, *d, r, *e, c0, c1, in_or_out, distance, flag);
+  return launch_check("lbm_domain_element");
+}
+
+int lbm_domain_clean(const lbm_domain* d, const double* in_or_out, double* distance, int32_t* flag, void* stream) {
+  int rc = check_domain(d, "lbm_domain_clean");
+  if (rc) return rc;
+  if (!in_or_out || !distance || !flag) return fail(LBM_ERR_ARG, "lbm_domain_clean: NULL array");
+  Box b = make_box(*d);
+  k_clean<<<blocks_for(b.nodes * b.nu), kThreads, 0, (cudaStream_t)stream>>>(b, in_or_out, distance, flag);
+  return launch_check("lbm_domain_clean");
+}
+
+int lbm_links_count(const lbm_domain* d, const int32_t* flag, int32_t u, int32_t label, int32_t* block_counts,
+                    void* stream) {
+  int rc = check_domain(d, "lbm_links_count");
+  if (rc) return rc;
+  if (!flag || !block_counts || u < 0 || u >= d->nu) return fail(LBM_ERR_ARG, "lbm_links_count: bad argument");
+  Box b = make_box(*d);
+  k_links_count<<<blocks_for(b.nodes), kThreads, 0, (cudaStream_t)stream>>>(b, flag, u, label, block_counts);
+  return launch_check("lbm_links_count");
+}
+
+int lbm_links_fill(const lbm_domain* d, const int32_t* flag, const double* distance, int32_t u, int32_t label,
+                   const int32_t* vsym, const int32_t* block_offsets, int32_t* rows, double* dist, void* stream) {
+  int rc = check_domain(d, "lbm_links_fill");
+  if (rc) return rc;
+  if (!flag || !distance || !vsym || !block_offsets || !rows || !dist || u < 0 || u >= d->nu)
+    return fail(LBM_ERR_ARG, "lbm_links_fill: bad argument");
+  Box b = make_box(*d);
+  int3 vs = make_int3(vsym[0], d->dim > 1 ? vsym[1] : 0, d->dim > 2 ? vsym[2] : 0);
+  k_links_fill<<<blocks_for(b.nodes), kThreads, 0, (cudaStream_t)stream>>>(b, flag, distance, u, label, vs,
+                                                                          block_offsets, rows, dist);
+  return launch_check("lbm_links_fill");
+}
+
+}  // extern "C"

@@ -28,7 +28,7 @@ class Domain:
     along every axis, whose ghost layers no boundary method writes.
     """
 
-    def __init__(self, dico, stencil=None, with_flags=True):
+    def __init__(self, dico, stencil=None, with_flags=True, device=False):
         self.valin = VALIN
         self.valout = VALOUT
         self.dim = _box_dim(dico)
@@ -73,6 +73,13 @@ class Domain:
             self.coords_halo.append(np.linspace(self.bounds[k][0] - beg, self.bounds[k][1] + beg,
                                                 self.global_size[k] + 2 * h))
         self.coords = [c[int(h):-int(h)] for c, h in zip(self.coords_halo, self.halo)]
+        self.device = bool(device) and with_flags
+        if self.device:
+            # the arrays are built and kept on the GPU (lbm_domain_* kernels);
+            # boundary links are extracted there too (link_list)
+            self.in_or_out = self.distance = self.flag = None
+            self._build_on_device()
+            return
         if not with_flags:
             if self.elements or any(l != -1 for l in self.box_label):
                 raise ValueError("a domain without flags must be periodic along every axis")
@@ -180,3 +187,119 @@ class Domain:
             sel = np.logical_and(self.distance[k] > 0, solid)
             self.distance[k][sel] = VALIN
             self.flag[k][sel] = VALIN
+
+    # ------------------------------------------------------------------ device construction
+    def _region(self, elem):
+        """Halo-coordinate region [nmin, nmax) an element touches (same rule as _add_element)."""
+        vmax = self.halo
+        lo, hi = elem.get_bounds()
+        origin = np.array([c[0] for c in self.coords_halo])
+        nmin = np.maximum(vmax, np.array((lo - origin) / self.dx, int) - vmax)
+        nmax = np.minimum(vmax + np.asarray(self.shape_in), np.array((hi - origin) / self.dx, int) + vmax + 1)
+        return nmin, nmax
+
+    def _element_desc(self, elem):
+        from . import geometry, runtime
+        e = runtime.ElementDesc()
+        if isinstance(elem, geometry.Circle):
+            e.kind = runtime.LBM_ELEMENT_CIRCLE
+            vals = [elem.center[0], elem.center[1], elem.radius]
+        elif isinstance(elem, geometry.Parallelogram):
+            e.kind = runtime.LBM_ELEMENT_PARALLELOGRAM
+            vals = [*elem.point, *elem.v1, *elem.v2]
+        else:
+            raise NotImplementedError(f"{type(elem).__name__} is not built on the device")
+        for i, v in enumerate(vals):
+            e.p[i] = float(v)
+        for i, lab in enumerate(elem.label[:4]):
+            e.label[i] = int(lab)
+        e.isfluid = int(elem.isfluid)
+        nmin, nmax = self._region(elem)
+        for a in range(self.dim):
+            e.lo[a], e.hi[a] = int(nmin[a]), int(nmax[a])
+        return e
+
+    def _build_on_device(self):
+        import ctypes
+        from . import runtime
+
+        core = runtime.core()
+        uv = self.stencil.unique_v
+        d = runtime.DomainDesc()
+        d.dim, d.nu, d.dx = self.dim, uv.shape[0], self.dx
+        shape = self.shape_halo + [1] * (3 - self.dim)
+        for a in range(3):
+            d.n[a] = shape[a]
+            d.halo[a] = int(self.halo[a]) if a < self.dim else 0
+        for u in range(uv.shape[0]):
+            for a in range(self.dim):
+                d.vel[u][a] = int(uv[u, a])
+        self._desc = d
+        self._nodes = int(np.prod(shape))
+        nu = uv.shape[0]
+        self.d_in_or_out = runtime.DeviceBuffer(8 * self._nodes)
+        self.d_distance = runtime.DeviceBuffer(8 * nu * self._nodes)
+        self.d_flag = runtime.DeviceBuffer(4 * nu * self._nodes)
+        self.d_coords = runtime.DeviceBuffer(8 * int(sum(shape[:self.dim])))
+        self.d_coords.upload(np.ascontiguousarray(np.concatenate(self.coords_halo), dtype=np.float64))
+        ref = ctypes.byref(d)
+        runtime.check(core.lbm_domain_reset(ref, self.d_in_or_out.handle, self.d_distance.handle,
+                                            self.d_flag.handle, None))
+        labels = np.asarray(self.box_label + [-2] * (6 - len(self.box_label)), dtype=np.int32)
+        runtime.check(core.lbm_domain_box(ref, labels.ctypes.data_as(ctypes.c_void_p), self.d_distance.handle,
+                                          self.d_flag.handle, None))
+        for elem in self.elements:
+            e = self._element_desc(elem)
+            runtime.check(core.lbm_domain_element(ref, ctypes.byref(e), self.d_coords.handle, self.d_in_or_out.handle,
+                                                  self.d_distance.handle, self.d_flag.handle, None))
+        runtime.check(core.lbm_domain_clean(ref, self.d_in_or_out.handle, self.d_distance.handle,
+                                            self.d_flag.handle, None))
+        runtime.check(core.lbm_device_synchronize())
+
+    def link_list(self, label, u, vsym):
+        """Nodes with flag[u] == label, row-major (np.where order), shifted by
+        vsym: (dim, count) int64 halo coordinates and their distances."""
+        import ctypes
+        from . import runtime
+
+        core = runtime.core()
+        ref = ctypes.byref(self._desc)
+        block = core.lbm_links_block()
+        nblocks = -(-self._nodes // block)
+        counts = runtime.DeviceBuffer(4 * nblocks)
+        runtime.check(core.lbm_links_count(ref, self.d_flag.handle, int(u), int(label), counts.handle, None))
+        host = np.empty(nblocks, dtype=np.int32)
+        counts.download(host)
+        offsets = np.zeros(nblocks, dtype=np.int32)
+        np.cumsum(host[:-1], out=offsets[1:])
+        total = int(host.sum())
+        if total == 0:
+            counts.free()
+            return np.zeros((self.dim, 0), dtype=np.int64), np.zeros(0)
+        counts.upload(offsets)
+        rows = runtime.DeviceBuffer(4 * total * self.dim)
+        dist = runtime.DeviceBuffer(8 * total)
+        vs = np.zeros(3, dtype=np.int32)
+        vs[:self.dim] = vsym
+        runtime.check(core.lbm_links_fill(ref, self.d_flag.handle, self.d_distance.handle, int(u), int(label),
+                                          vs.ctypes.data_as(ctypes.c_void_p), counts.handle, rows.handle,
+                                          dist.handle, None))
+        r = np.empty((total, self.dim), dtype=np.int32)
+        dd = np.empty(total)
+        rows.download(r)
+        dist.download(dd)
+        for b in (counts, rows, dist):
+            b.free()
+        return r.T.astype(np.int64), dd
+
+    def download_arrays(self):
+        """Host copies of the device arrays (in_or_out, distance, flag), as the host path builds them."""
+        nu = self._desc.nu
+        shape = self.shape_halo
+        ioo = np.empty(self._nodes)
+        dist = np.empty(nu * self._nodes)
+        flag = np.empty(nu * self._nodes, dtype=np.int32)
+        self.d_in_or_out.download(ioo)
+        self.d_distance.download(dist)
+        self.d_flag.download(flag)
+        return ioo.reshape(shape), dist.reshape([nu] + shape), flag.reshape([nu] + shape).astype(np.int64)

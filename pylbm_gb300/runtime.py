@@ -58,6 +58,32 @@ class Lattice(ctypes.Structure):
 
 LBM_MAX_PRM = 8
 LBM_INSTANCE_PAIRS = 1
+LBM_ELEMENT_CIRCLE = 1
+LBM_ELEMENT_PARALLELOGRAM = 2
+
+
+class DomainDesc(ctypes.Structure):
+    """lbm_domain (include/lbm_gb300.h)."""
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("nu", ctypes.c_int32),
+        ("n", ctypes.c_int32 * 3),
+        ("halo", ctypes.c_int32 * 3),
+        ("vel", (ctypes.c_int32 * 3) * LBM_MAX_Q),
+        ("dx", ctypes.c_double),
+    ]
+
+
+class ElementDesc(ctypes.Structure):
+    """lbm_element (include/lbm_gb300.h)."""
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("isfluid", ctypes.c_int32),
+        ("label", ctypes.c_int32 * 4),
+        ("p", ctypes.c_double * 8),
+        ("lo", ctypes.c_int32 * 3),
+        ("hi", ctypes.c_int32 * 3),
+    ]
 
 
 class Instance(ctypes.Structure):
@@ -112,7 +138,7 @@ def _nvcc_shared(sources, out, extra=()):
 
 def build_core(force=False):
     out = os.path.join(LIB_DIR, CORE_NAME)
-    srcs = [os.path.join(CSRC, "lbm_core.cu"), os.path.join(CSRC, "lbm_closure.cu")]
+    srcs = [os.path.join(CSRC, "lbm_core.cu"), os.path.join(CSRC, "lbm_closure.cu"), os.path.join(CSRC, "lbm_domain.cu")]
     deps = srcs + [os.path.join(CSRC, f) for f in ("lbm_common.cuh", "lbm_mlp.cuh")] + \
         [os.path.join(INCLUDE, "lbm_gb300.h")]
     if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
@@ -171,6 +197,14 @@ def core():
             _sig(lib, "lbm_anti_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_neumann", I32, [P, P, P, I32, LP, I32, P])
             _sig(lib, "lbm_bouzidi_bounce_back", I32, [P, P, P, P, I32, P, P, LP, P, P])
+            DP = ctypes.POINTER(DomainDesc)
+            _sig(lib, "lbm_domain_reset", I32, [DP, P, P, P, P])
+            _sig(lib, "lbm_domain_box", I32, [DP, P, P, P, P])
+            _sig(lib, "lbm_domain_element", I32, [DP, ctypes.POINTER(ElementDesc), P, P, P, P, P])
+            _sig(lib, "lbm_domain_clean", I32, [DP, P, P, P, P])
+            _sig(lib, "lbm_links_block", I32, [])
+            _sig(lib, "lbm_links_count", I32, [DP, P, I32, I32, P, P])
+            _sig(lib, "lbm_links_fill", I32, [DP, P, P, I32, I32, P, P, P, P, P])
             _sig(lib, "lbm_bouzidi_anti_bounce_back", I32, [P, P, P, P, I32, P, P, LP, I32, P])
             _sig(lib, "lbm_population_sums_scratch_bytes", I32, [LP, ctypes.POINTER(SZ)])
             _sig(lib, "lbm_population_sums", I32, [P, LP, P, P, P, SZ, P])

@@ -111,10 +111,15 @@ class Simulation:
     c0 : sequence of float or None
         reference state of the conserved moments for shifted storage
         (default: the mean of the initial fields, 4 significant digits).
+    device_domain : bool
+        build the fluid/solid map, wall distances and boundary link lists on
+        the GPU (identical to the host construction; for large obstacle
+        sets); ``domain.in_or_out``/``distance``/``flag`` then stay on the
+        device (``domain.download_arrays()``).
     """
 
     def __init__(self, dico, sorder=None, dtype="float64", check_inverse=False, initialize=True,
-                 shifted=None, parity=True, node_pairs=True, c0=None):
+                 shifted=None, parity=True, node_pairs=True, c0=None, device_domain=False):
         gen = str(dico.get("generator", "cuda")).upper()
         if gen != "CUDA":
             raise ValueError(f"pylbm_gb300 implements generator='cuda', not {gen!r}")
@@ -129,7 +134,7 @@ class Simulation:
         lab = [lab] if isinstance(lab, (int, np.integer)) else list(lab)
         all_periodic = all(int(l) == -1 for l in lab) and not dico.get("elements")
         # wall distances and flags only matter where some boundary method needs them
-        self.domain = Domain(dico, self.scheme.stencil, with_flags=not all_periodic)
+        self.domain = Domain(dico, self.scheme.stencil, with_flags=not all_periodic, device=device_domain)
         if self.domain.dim != self.scheme.dim:
             raise ValueError("the dimension of the domain and of the scheme are not the same")
         self.dim = self.domain.dim

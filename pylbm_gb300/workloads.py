@@ -201,3 +201,56 @@ def shear_layer(n=256, nu=1e-3, u0=0.05, width=1.0 / 80.0, delta=0.05, omega=Non
         "init": {RHO: 1.0, QX: qx_init, QY: qy_init},
         "generator": generator,
     }
+
+
+def geier_d2q9(dx, la=1.0, rho_o=1.0, mu=5.0e-6, zeta=5.0e-5):
+    """D2Q9 Geier basis with relative velocity q/rho: central moments (pylbm's
+    2D Navier-Stokes demos, moments_choice "Geier"); rates from the bulk and
+    shear viscosities."""
+    ux, uy = QX / RHO, QY / RHO
+    rhou2 = RHO * (ux**2 + uy**2)
+    c = 3.0 / (la * rho_o * dx)
+    s_1 = 1 / (0.5 + c * (zeta - 2 * mu / 3))
+    s_2 = 1 / (0.5 + c * mu)
+    return {
+        "velocities": list(range(9)),
+        "polynomials": [1, X, Y, X**2 + Y**2, X * Y**2, Y * X**2, X**2 * Y**2, X**2 - Y**2, X * Y],
+        "relaxation_parameters": [0.0, 0.0, 0.0, s_1, s_1, s_1, s_1, s_2, s_2],
+        "equilibrium": [RHO, QX, QY, rhou2 + 2 / 3 * RHO * LA**2, QX * (LA**2 / 3 + uy**2),
+                        QY * (LA**2 / 3 + ux**2), RHO * (LA**2 / 3 + ux**2) * (LA**2 / 3 + uy**2),
+                        RHO * (ux**2 - uy**2), RHO * ux * uy],
+        "conserved_moments": [RHO, QX, QY],
+    }
+
+
+def karman(dx=1.0 / 64, u_o=0.05, mu=5.0e-6, bc=None, circle=None, generator="cuda"):
+    """Flow past a disc in a channel, D2Q9 Geier with relative velocity and
+    Bouzidi walls (the physics of pylbm's demo/2D/Karman_vortex_street.py at
+    any resolution): box [0, 2] x [0, 1], disc of radius 1/32 at
+    (0.3, 0.5 + 2 dx), inflow state on label 0, NeumannX outflow."""
+    bc = _bc(bc)
+    if circle is None:
+        from .geometry import Circle as circle
+    rho_o, la = 1.0, 1.0
+
+    def bc_in(f, m, x, y, rho_o, u_o):
+        m[RHO] = rho_o
+        m[QX] = rho_o * u_o
+        m[QY] = 0.0
+
+    return {
+        "box": {"x": [0.0, 2.0], "y": [0.0, 1.0], "label": [0, 1, 0, 0]},
+        "elements": [circle([0.3, 0.5 + 2 * dx], 1.0 / 32, label=2)],
+        "space_step": dx,
+        "scheme_velocity": la,
+        "schemes": [geier_d2q9(dx, la, rho_o, mu, 10 * mu)],
+        "parameters": {LA: la},
+        "init": {RHO: rho_o, QX: rho_o * u_o, QY: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack}, "value": (bc_in, (rho_o, u_o))},
+            1: {"method": {0: bc.NeumannX}},
+            2: {"method": {0: bc.BouzidiBounceBack}},
+        },
+        "generator": generator,
+        "relative_velocity": [QX / RHO, QY / RHO],
+    }
