@@ -58,29 +58,27 @@ class ExprPrinter:
         if e.is_Symbol:
             raise SchemeError(f"unbound symbol {e} in generated expression")
         if e.is_Add:
-            # product terms after the first fold into explicit multiply-adds:
-            # c*x -> fma(c, x, acc), x*y*z -> fma(x, y*z, acc), -x*y -> fma(-x, y, acc)
-            acc = None
+            # every product term is an explicit multiply-add: the plain terms
+            # are summed first, then c*x -> fma(c, x, acc), x*y*z -> fma(x, y*z, acc),
+            # -x*y -> fma(-x, y, acc), x^n -> fma(x, x^(n-1), acc); no product
+            # ever feeds an addition, so there is nothing left to contract
+            plain, prods = [], []
             for a in e.args:
-                coef, rest = a.as_coeff_Mul()
-                if acc is None:
-                    acc = self.p(a)
-                elif coef.is_Number and coef not in (1, -1) and rest != 1:
-                    acc = f"lbm_fma<R>({self.p(coef)}, {self.p(rest)}, {acc})"
-                elif rest.is_Mul and self._splittable(rest):
-                    first, tail = self._split(rest)
-                    lead = first if coef == 1 else f"(-{first})"
-                    acc = f"lbm_fma<R>({lead}, {tail}, {acc})"
-                elif rest.is_Pow and rest.exp.is_Integer and rest.exp >= 2:
-                    first = self.p(rest.base)
-                    lead = first if coef == 1 else f"(-{first})"
-                    acc = f"lbm_fma<R>({lead}, {self.p(sp.Pow(rest.base, rest.exp - 1))}, {acc})"
-                elif coef == -1:
-                    acc = f"({acc} - {self.p(rest)})"
-                else:
-                    acc = f"({acc} + {self.p(a)})"
+                (prods if self._fusable(a) else plain).append(a)
+            if plain:
+                acc = self.p(plain[0])
+                for a in plain[1:]:
+                    coef, rest = a.as_coeff_Mul()
+                    acc = f"({acc} - {self.p(rest)})" if coef == -1 else f"({acc} + {self.p(a)})"
+            else:
+                acc, prods = self.p(prods[0]), prods[1:]
+            for a in prods:
+                acc = self._fma_term(a, acc)
             return "(" + acc + ")"
         if e.is_Mul:
+            coef, rest = e.as_coeff_Mul()
+            if coef == -1:  # a negation, not a multiplication
+                return f"(-{self.p(rest)})"
             num, den = self._mul_parts(e)
             s = "*".join(num) if num else "LBM_R(1)"
             if den:
@@ -118,10 +116,52 @@ class ExprPrinter:
         num, den = self._mul_parts(e)
         return not den and len(num) >= 2
 
+    def _fusable(self, a):
+        """A term c*x, x*y*..., or x^n that folds into a multiply-add."""
+        coef, rest = a.as_coeff_Mul()
+        if coef.is_Number and coef not in (1, -1) and rest != 1:
+            return True
+        if rest.is_Mul and self._splittable(rest):
+            return True
+        return bool(rest.is_Pow and rest.exp.is_Integer and rest.exp >= 2)
+
+    def _fma_term(self, a, acc):
+        coef, rest = a.as_coeff_Mul()
+        if coef.is_Number and coef not in (1, -1) and rest != 1:
+            return f"lbm_fma<R>({self.p(coef)}, {self.p(rest)}, {acc})"
+        if rest.is_Mul:
+            first, tail = self._split(rest)
+        else:
+            first, tail = self.p(rest.base), self.p(sp.Pow(rest.base, rest.exp - 1))
+        lead = first if coef == 1 else f"(-{first})"
+        return f"lbm_fma<R>({lead}, {tail}, {acc})"
+
     def _split(self, e):
         """x*y*z -> ("x", "(y*z)") for a product without divisions."""
         num, _ = self._mul_parts(e)
         return num[0], "(" + "*".join(num[1:]) + ")"
+
+
+def _cse(exprs, prefix):
+    """Common subexpressions of sums only.
+
+    A shared product t = x*y would reach an addition as a plain value (t + z),
+    a pattern the compiler may or may not fuse into one multiply-add, and in
+    practice fuses for packed FP32x2 operations even when both are written
+    with an explicit rounding mode.  Products are therefore substituted back
+    into the expressions, where the printer turns every product term of a sum
+    into an explicit lbm_fma, and both the scalar and the two-node kernels
+    round identically.
+    """
+    repl, red = sp.cse(exprs, symbols=sp.numbered_symbols(prefix), optimizations="basic")
+    keep, back = [], {}
+    for sym, val in repl:
+        val = val.xreplace(back)
+        if val.is_Mul or val.is_Pow:
+            back[sym] = val
+        else:
+            keep.append((sym, sp.expand(val)))
+    return keep, [sp.expand(r.xreplace(back)) for r in red]
 
 
 def _pairs(scheme):
@@ -334,7 +374,7 @@ class SchemeSource:
             else:
                 d = sp.expand(e.subs({cons[c]: dsym[c] for c in range(nc)}))
             exprs.append(d)
-        repl, red = sp.cse(exprs, symbols=sp.numbered_symbols("t_"), optimizations="basic")
+        repl, red = _cse(exprs, "t_")
         lines = []
         pr = ExprPrinter(names)
         for sym, val in repl:
@@ -354,7 +394,10 @@ class SchemeSource:
             elif red[idx] == 0:  # m + s (0 - m) = fma(-s, m, m), the same rounding
                 lines.append(f"{indent}{m}[{k}] = lbm_fma<R>(-({sstr}), {m}[{k}], {m}[{k}]);")
             else:
-                lines.append(f"{indent}{m}[{k}] = lbm_fma<R>({sstr}, ({eqs} - {m}[{k}]), {m}[{k}]);")
+                # eq - m printed as one sum, so a product in eq becomes fma(., ., -m)
+                mk = sp.Symbol(f"__m{k}")
+                names[mk] = f"{m}[{k}]"
+                lines.append(f"{indent}{m}[{k}] = lbm_fma<R>({sstr}, {pr(red[idx] - mk)}, {m}[{k}]);")
         return lines
 
     def _eq_abs_code(self, m, indent="  "):
@@ -366,7 +409,7 @@ class SchemeSource:
         for i, s in enumerate(self.params):
             names[s] = f"prm[{i}]"
         exprs = [sc.EQ[k] for k in range(nc, sc.nv)]
-        repl, red = sp.cse(exprs, symbols=sp.numbered_symbols("u_"), optimizations="basic")
+        repl, red = _cse(exprs, "u_")
         pr = ExprPrinter(names)
         lines = []
         for sym, val in repl:
@@ -396,7 +439,7 @@ class SchemeSource:
 
     def _assign_block(self, targets, exprs, names, prefix, indent):
         """targets[i] = exprs[i] evaluated together (all right-hand sides first)."""
-        repl, red = sp.cse(exprs, symbols=sp.numbered_symbols(f"{prefix}c_"), optimizations="basic")
+        repl, red = _cse(exprs, f"{prefix}c_")
         pr = ExprPrinter(dict(names))
         lines = [f"{indent}{{"]
         for sym, val in repl:

@@ -103,18 +103,21 @@ struct F2 {
   __device__ __forceinline__ explicit F2(int a) { v = make_float2((float)a, (float)a); }
 };
 
-// The packed operations are written as PTX with an explicit rounding mode:
-// ptxas never contracts .rn-qualified instructions, so a packed multiply
-// followed by a packed add stays two roundings, exactly as the scalar code
-// of a module built with -fmad=false.
-#define LBM_F2_OP2(OP)                                                                          \
-  asm("{\n\t.reg .b64 A, B, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t" OP            \
-      " D, A, B;\n\tmov.b64 {%0, %1}, D;\n\t}"                                                  \
-      : "=f"(r.v.x), "=f"(r.v.y)                                                                \
-      : "f"(a.v.x), "f"(a.v.y), "f"(b.v.x), "f"(b.v.y))
-__device__ __forceinline__ F2 operator+(F2 a, F2 b) { F2 r; LBM_F2_OP2("add.rn.f32x2"); return r; }
-__device__ __forceinline__ F2 operator*(F2 a, F2 b) { F2 r; LBM_F2_OP2("mul.rn.f32x2"); return r; }
-#undef LBM_F2_OP2
+// Adds and multiply-adds are packed.  A packed multiply whose result feeds a
+// packed add is fused into one multiply-add by ptxas on sm_103a even when
+// both carry an explicit .rn (measured: the pair then rounds once), while
+// the scalar code of a module built with -fmad=false rounds twice; products
+// are therefore two scalar multiplies, which are never contracted, and the
+// two-node kernels round exactly as the one-node kernels.
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) {
+  F2 r;
+  asm("{\n\t.reg .b64 A, B, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t"
+      "add.rn.f32x2 D, A, B;\n\tmov.b64 {%0, %1}, D;\n\t}"
+      : "=f"(r.v.x), "=f"(r.v.y)
+      : "f"(a.v.x), "f"(a.v.y), "f"(b.v.x), "f"(b.v.y));
+  return r;
+}
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2(__fmul_rn(a.v.x, b.v.x), __fmul_rn(a.v.y, b.v.y)); }
 __device__ __forceinline__ F2 operator-(F2 a) { return F2(-a.v.x, -a.v.y); }
 __device__ __forceinline__ F2 operator-(F2 a, F2 b) { return a + (-b); }
 __device__ __forceinline__ F2 operator/(F2 a, F2 b) { return F2(a.v.x / b.v.x, a.v.y / b.v.y); }
