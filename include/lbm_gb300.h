@@ -165,6 +165,35 @@ int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* 
                                  int32_t ncond, const double* rhs, const double* dist, const lbm_lattice* lat,
                                  int32_t ordered, void* stream);
 
+/* Every boundary method of a step in one launch.  `methods` (device,
+ * nmethods entries) describes each method's lists as for the calls above;
+ * link c of the batch belongs to the method whose [first, first + ncond)
+ * holds c.  All links read the populations as they are before the call, so
+ * the batch equals the methods applied one after the other only when no
+ * link loads a population that a link of the batch stores (the caller
+ * checks; pylbm's lists for a wall, an inflow and an outflow satisfy it).
+ * Ordered (sequential) methods are not batched. */
+#define LBM_BC_BOUNCE_BACK 1
+#define LBM_BC_ANTI_BOUNCE_BACK 2
+#define LBM_BC_NEUMANN 3
+#define LBM_BC_BOUZIDI_BOUNCE_BACK 4
+#define LBM_BC_BOUZIDI_ANTI_BOUNCE_BACK 5
+
+typedef struct lbm_bc_method {
+  int32_t kind;               /* LBM_BC_* */
+  int32_t ncond;
+  int32_t first;              /* index of the method's first link in the batch */
+  int32_t reserved;
+  const int32_t* iload0;
+  const int32_t* iload1;      /* Bouzidi only */
+  const int32_t* istore;
+  const double* rhs;          /* not for Neumann */
+  const double* dist;         /* Bouzidi only */
+} lbm_bc_method;
+
+int lbm_boundary_batch(void* f, const lbm_lattice* lat, const lbm_bc_method* methods, int32_t nmethods,
+                       int32_t total_links, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* Domain construction on the device (pylbm/domain.py:87-620 and the  */
 /* link lists of pylbm/boundary.py:23-160): fluid/solid map, per-link */

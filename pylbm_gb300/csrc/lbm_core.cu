@@ -166,6 +166,44 @@ __global__ void k_bouzidi_ordered(S* __restrict__ f, Geo g, BouzidiArgs a) {
     for (int c = 0; c < a.ncond; ++c) bouzidi_store(f, g, a, c, bouzidi_value(f, g, a, c));
 }
 
+// ---------------------------------------------------------------- batched boundary methods
+struct BatchArgs {
+  const lbm_bc_method* methods;
+  int nmethods;
+  int total;
+  double shift[LBM_MAX_Q];
+};
+
+// one thread per link of the batch; the same arithmetic as the per-method kernels
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_boundary_batch(S* __restrict__ f, Geo g, BatchArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.total) return;
+  int m = 0;
+  while (m + 1 < a.nmethods && c >= a.methods[m + 1].first) ++m;
+  const lbm_bc_method M = a.methods[m];
+  const int l = c - M.first;
+  const int w = g.dim + 1;
+  int ks, k0;
+  const long long os = link_slot(g, M.istore + (long long)l * w, ks);
+  const long long o0 = link_slot(g, M.iload0 + (long long)l * w, k0);
+  const double f0 = (double)Store<S>::load_plain(f + o0) + a.shift[k0];
+  double v;
+  if (M.kind == LBM_BC_BOUZIDI_BOUNCE_BACK || M.kind == LBM_BC_BOUZIDI_ANTI_BOUNCE_BACK) {
+    int k1;
+    const long long o1 = link_slot(g, M.iload1 + (long long)l * w, k1);
+    const double f1 = (double)Store<S>::load_plain(f + o1) + a.shift[k1];
+    const double d = M.dist[l];
+    const double t1 = __dmul_rn(__dsub_rn(1.0, d), f1);
+    const double t0 = __dmul_rn(d, f0);
+    v = __dadd_rn(M.kind == LBM_BC_BOUZIDI_ANTI_BOUNCE_BACK ? __dsub_rn(t1, t0) : __dadd_rn(t1, t0), M.rhs[l]);
+  } else {
+    const double sign = M.kind == LBM_BC_ANTI_BOUNCE_BACK ? -1.0 : 1.0;
+    v = sign * f0 + (M.kind == LBM_BC_NEUMANN ? 0.0 : M.rhs[l]);
+  }
+  Store<S>::store(f + os, (decltype(Store<S>::load_plain(f)))(v - a.shift[ks]));
+}
+
 // ---------------------------------------------------------------- sums
 // Stage 1: block b of population k sums rows [b*rows_per_block, ...) of the
 // interior with FP64 warp shuffles; stage 2 adds the per-block partials.
@@ -601,6 +639,27 @@ static int bouzidi_common(void* f, const int32_t* iload0, const int32_t* iload1,
       k_bouzidi<S><<<blocks, kThreads, 0, s>>>((S*)f, g, a);
     }
     return launch_check(who);
+  });
+}
+
+int lbm_boundary_batch(void* f, const lbm_lattice* lat, const lbm_bc_method* methods, int32_t nmethods,
+                       int32_t total_links, void* stream) {
+  int rc = check_lattice(lat, "lbm_boundary_batch");
+  if (rc) return rc;
+  if (total_links < 0 || nmethods < 0) return fail(LBM_ERR_ARG, "lbm_boundary_batch: negative size");
+  if (total_links == 0) return LBM_OK;
+  if (!f || !methods || nmethods == 0) return fail(LBM_ERR_ARG, "lbm_boundary_batch: NULL argument");
+  BatchArgs a;
+  a.methods = methods;
+  a.nmethods = nmethods;
+  a.total = total_links;
+  for (int k = 0; k < LBM_MAX_Q; ++k) a.shift[k] = k < lat->nv ? lat->shift[k] : 0.0;
+  Geo g = make_geo(*lat);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    k_boundary_batch<S><<<(total_links + kThreads - 1) / kThreads, kThreads, 0, s>>>((S*)f, g, a);
+    return launch_check("lbm_boundary_batch");
   });
 }
 

@@ -74,6 +74,25 @@ class DomainDesc(ctypes.Structure):
     ]
 
 
+LBM_BC_KIND = {"bounce_back": 1, "anti_bounce_back": 2, "neumann": 3, "bouzidi_bounce_back": 4,
+               "bouzidi_anti_bounce_back": 5}
+
+
+class BcMethod(ctypes.Structure):
+    """lbm_bc_method (include/lbm_gb300.h)."""
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("ncond", ctypes.c_int32),
+        ("first", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("iload0", ctypes.c_void_p),
+        ("iload1", ctypes.c_void_p),
+        ("istore", ctypes.c_void_p),
+        ("rhs", ctypes.c_void_p),
+        ("dist", ctypes.c_void_p),
+    ]
+
+
 class ElementDesc(ctypes.Structure):
     """lbm_element (include/lbm_gb300.h)."""
     _fields_ = [
@@ -205,6 +224,7 @@ def core():
             _sig(lib, "lbm_links_block", I32, [])
             _sig(lib, "lbm_links_count", I32, [DP, P, I32, I32, P, P])
             _sig(lib, "lbm_links_fill", I32, [DP, P, P, I32, I32, P, P, P, P, P])
+            _sig(lib, "lbm_boundary_batch", I32, [P, LP, P, I32, I32, P])
             _sig(lib, "lbm_bouzidi_anti_bounce_back", I32, [P, P, P, P, I32, P, P, LP, I32, P])
             _sig(lib, "lbm_population_sums_scratch_bytes", I32, [LP, ctypes.POINTER(SZ)])
             _sig(lib, "lbm_population_sums", I32, [P, LP, P, P, P, SZ, P])

@@ -169,6 +169,8 @@ class Simulation:
         self._m_cache = {}
         self._update_m = True
         self._bc_dev = []
+        self._bc_batch = None
+        self.batch_boundary = True  # one launch for all boundary methods where the lists allow it
         self._graph = None
         self._graph_key = None
         self._need_init = True
@@ -315,6 +317,7 @@ class Simulation:
                 # copy semantics of the bounce-back: compute every link before storing
                 dev["scratch"] = runtime.DeviceBuffer(8 * max(meth.ncond, 1)) if dev["ordered"] else None
             self._bc_dev.append((meth, dev))
+        self._bc_batch = self._batch_table()
 
     @staticmethod
     def _links_independent(meth):
@@ -322,10 +325,42 @@ class Simulation:
         st = {tuple(r) for r in meth.istore.tolist()}
         return not any(tuple(r) in st for il in meth.iload for r in il.tolist())
 
+    def _batch_table(self):
+        """Device table of every method for one lbm_boundary_batch launch, or
+        None when some link of one method loads a slot another link stores
+        (then the methods run one after the other, as pylbm applies them)."""
+        if len(self._bc_dev) < 2:
+            return None
+        stores = set()
+        for meth, _ in self._bc_dev:
+            stores.update(map(tuple, meth.istore.tolist()))
+        for meth, _ in self._bc_dev:
+            if any(tuple(r) in stores for il in meth.iload for r in il.tolist()):
+                return None
+        table = (runtime.BcMethod * len(self._bc_dev))()
+        first = 0
+        for i, (meth, dev) in enumerate(self._bc_dev):
+            t = table[i]
+            t.kind, t.ncond, t.first = runtime.LBM_BC_KIND[meth.kind], meth.ncond, first
+            t.iload0 = dev["iload"][0].ptr
+            t.iload1 = dev["iload"][1].ptr if len(dev["iload"]) > 1 else None
+            t.istore, t.rhs = dev["istore"].ptr, dev["rhs"].ptr
+            t.dist = dev["dist"].ptr if "dist" in dev else None
+            first += meth.ncond
+        buf = runtime.DeviceBuffer(ctypes.sizeof(table))
+        runtime.check(self._core.lbm_memcpy(buf.handle, ctypes.cast(table, ctypes.c_void_p), ctypes.sizeof(table),
+                                            runtime.H2D, self._stream))
+        self.synchronize()
+        return buf, len(self._bc_dev), first
+
     # ------------------------------------------------------------------ step
     def _enqueue_boundary(self, F):
         lat = ctypes.byref(self._lat)
         runtime.check(self._core.lbm_update_halo(F.handle, lat, self._stream))
+        if self._bc_batch is not None and self.batch_boundary:
+            buf, nmeth, total = self._bc_batch
+            runtime.check(self._core.lbm_boundary_batch(F.handle, lat, buf.handle, nmeth, total, self._stream))
+            return
         for meth, dev in self._bc_dev:
             il, st, rhs, ordered = dev["iload"], dev["istore"].handle, dev["rhs"].handle, dev["ordered"]
             if meth.kind == "bounce_back":
@@ -559,6 +594,9 @@ class Simulation:
                     if isinstance(b, runtime.DeviceBuffer):
                         b.free()
         self._bc_dev = []
+        if self._bc_batch is not None:
+            self._bc_batch[0].free()
+            self._bc_batch = None
         if self._stream:
             self._core.lbm_stream_destroy(self._stream)
             self._stream = None

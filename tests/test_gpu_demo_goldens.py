@@ -54,3 +54,20 @@ def test_h5_output_matches_reference_golden_file(tmp_path):
         assert np.all(diff <= np.maximum(1e-14 * np.abs(ref), 1e-7)), key
     assert (tmp_path / "poiseuille.xdmf").exists()
     sim.free()
+
+
+@pytest.mark.parametrize("name", ["karman_vortex_street", "poiseuille", "air_conditioning"])
+def test_batched_boundary_launch_equals_per_method(name):
+    """All boundary methods in one launch give the per-method result bit for bit."""
+    build, final_time, _, fields = demo_cases.CASES[name]
+    out = []
+    for batch in (True, False):
+        sim = Simulation(build())
+        sim.batch_boundary = batch
+        sim.run(20)
+        out.append(np.array([sim.m[k] for k in range(sim.scheme.nv)]))
+        batched = sim._bc_batch is not None
+        sim.free()
+    assert np.array_equal(out[0], out[1])
+    if name == "karman_vortex_street":
+        assert batched  # wall, inflow, outflow and disc lists are independent
