@@ -143,3 +143,68 @@ class Parallelogram(Element):
             border[closer] = lab
         alpha[alpha == _FAR] = -1.0
         return alpha, border
+
+
+class Sphere(Element):
+    """Ball obstacle (pylbm/elements/sphere.py:24); the surface counts as inside.
+
+    The ray distance follows the ellipsoid quadratic of pylbm
+    (pylbm/elements/utils.py:171 ``distance_ellipsoid``) with the three
+    semi-axes r e_x, r e_y, r e_z, term by term in the same order.
+    """
+
+    number_of_bounds = 1
+
+    def __init__(self, center, radius, label=0, isfluid=False):
+        if radius < 0:
+            raise ValueError("the radius of the sphere should be positive")
+        self.dim = 3
+        self.center = np.asarray(center, dtype=np.float64)
+        self.radius = float(radius)
+        super().__init__(label, isfluid)
+
+    def get_bounds(self):
+        return self.center - self.radius, self.center + self.radius
+
+    def point_inside(self, grid):
+        x, y, z = grid
+        return ((x - self.center[0]) ** 2 + (y - self.center[1]) ** 2 + (z - self.center[2]) ** 2) <= self.radius ** 2
+
+    def distance(self, grid, v, dmax=None):
+        x, y, z = grid
+        shape = (x.size, y.size, z.size)
+        r = self.radius
+        e1, e2, e3 = r * np.array([1, 0, 0]), r * np.array([0, 1, 0]), r * np.array([0, 0, 1])
+        X, Y, Z = x - self.center[0], y - self.center[1], z - self.center[2]
+        c12, c23, c31 = np.cross(e1, e2), np.cross(e2, e3), np.cross(e3, e1)
+        dd = np.inner(e1, c23) ** 2
+        cxx = c12[0] ** 2 + c23[0] ** 2 + c31[0] ** 2
+        cyy = c12[1] ** 2 + c23[1] ** 2 + c31[1] ** 2
+        czz = c12[2] ** 2 + c23[2] ** 2 + c31[2] ** 2
+        cxy = 2 * (c12[0] * c12[1] + c23[0] * c23[1] + c31[0] * c31[1])
+        cyz = 2 * (c12[1] * c12[2] + c23[1] * c23[2] + c31[1] * c31[2])
+        czx = 2 * (c12[2] * c12[0] + c23[2] * c23[0] + c31[2] * c31[0])
+        qa = cxx * v[0] ** 2 + cyy * v[1] ** 2 + czz * v[2] ** 2 + cxy * v[0] * v[1] + cyz * v[1] * v[2] \
+            + czx * v[2] * v[0]
+        qb = (2 * cxx * v[0] + cxy * v[1] + czx * v[2]) * X + (2 * cyy * v[1] + cyz * v[2] + cxy * v[0]) * Y \
+            + (2 * czz * v[2] + czx * v[0] + cyz * v[1]) * Z
+        qc = cxx * X ** 2 + cyy * Y ** 2 + czz * Z ** 2 + cxy * X * Y + cyz * Y * Z + czx * Z * X - dd
+        disc = np.broadcast_to(qb ** 2 - 4 * qa * qc, shape).copy()
+        ok = disc >= 0
+        disc[ok] = np.sqrt(disc[ok])
+        qbb = np.broadcast_to(qb, shape)
+        t1 = np.full(shape, _FAR)
+        t2 = np.full(shape, _FAR)
+        t1[ok] = (-qbb[ok] - disc[ok]) / (2 * qa)
+        t2[ok] = (-qbb[ok] + disc[ok]) / (2 * qa)
+        t1[t1 < 0] = _FAR
+        t2[t2 < 0] = _FAR
+        t = -np.ones(shape)
+        t[ok] = np.minimum(t1[ok], t2[ok])
+        t[t == _FAR] = -1
+        hit = t > 0 if dmax is None else np.logical_and(t > 0, t <= dmax)
+        alpha = -np.ones(shape)
+        border = -np.ones(shape)
+        alpha[hit] = t[hit]
+        border[hit] = self.label[0]
+        return alpha, border

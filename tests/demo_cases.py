@@ -982,3 +982,55 @@ CASES.update({
     "d1q5_advection": (d1q5_advection, 0.5, None, {"u": "u"}),
     "d2q13_advection": (d2q13_advection, 0.25, None, {"u": "u"}),
 })
+
+
+def karman_3d(dx=1.0 / 32, bc=None, sphere=None, generator="cuda"):
+    """Flow past a sphere, D3Q15 MRT (demo/3D/Karman.py:29-125), Re 2000.
+
+    Box [0, 2] x [0, 1]^2 periodic in y and z; inflow (label 1) Bouzidi
+    bounce-back with qx = 0.01, outflow (label 2) NeumannX, sphere of radius
+    1/8 at (0.3, 0.5, 0.5) (label 0) Bouzidi bounce-back.  pylbm has no golden
+    file for it; the fixture is the reference run (space step 1/32).
+    """
+    bc = _bc(bc)
+    if sphere is None:
+        from pylbm_gb300.geometry import Sphere as sphere
+    mass, qx, qy, qz = sp.symbols("mass, qx, qy, qz")
+    la_c = sp.Symbol("lambda")
+    nu = 5.0 / 2000
+    s1, s2, s4 = 1.6, 1.2, 1.6
+    s9 = 1.0 / (3 * nu + 0.5)
+    s11, s14 = s9, 1.2
+    r = X**2 + Y**2 + Z**2
+
+    def bc_up(f, m, x, y, z):
+        m[qx] = 0.01
+
+    return {
+        "box": {"x": [0.0, 2.0], "y": [0.0, 1.0], "z": [0.0, 1.0], "label": [1, 2, -1, -1, -1, -1]},
+        "elements": [sphere((0.3, 0.5, 0.5), 0.125, 0)],
+        "space_step": dx,
+        "scheme_velocity": 1.0,
+        "schemes": [{
+            "velocities": list(range(7)) + list(range(19, 27)),
+            "conserved_moments": [mass, qx, qy, qz],
+            "polynomials": [1, r - 2, 0.5 * (15 * r**2 - 55 * r + 32), X, 0.5 * (5 * r - 13) * X, Y,
+                            0.5 * (5 * r - 13) * Y, Z, 0.5 * (5 * r - 13) * Z, 3 * X**2 - r, Y**2 - Z**2,
+                            X * Y, Y * Z, Z * X, X * Y * Z],
+            "relaxation_parameters": [0, s1, s2, 0, s4, 0, s4, 0, s4, s9, s9, s11, s11, s11, s14],
+            "equilibrium": [mass, -mass + qx**2 + qy**2 + qz**2, -mass, qx, -7.0 / 3 * qx, qy, -7.0 / 3 * qy, qz,
+                            -7.0 / 3 * qz, 1.0 / 3 * (2 * qx**2 - (qy**2 + qz**2)), qy**2 - qz**2, qx * qy,
+                            qy * qz, qz * qx, 0],
+        }],
+        "init": {mass: 1.0, qx: 0.0, qy: 0.0, qz: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BouzidiBounceBack}},
+            1: {"method": {0: bc.BouzidiBounceBack}, "value": bc_up},
+            2: {"method": {0: bc.NeumannX}},
+        },
+        "parameters": {la_c: 1.0},
+        "generator": generator,
+    }
+
+
+CASES["karman_3d"] = (karman_3d, 0.25, None, {"mass": "mass", "qx": "qx", "qy": "qy", "qz": "qz"})

@@ -55,8 +55,8 @@ def make(name):
     if h5name is not None:
         gold = h5lite.read(os.path.join(REFERENCE, "tests", "reference", h5name + ".h5"))
         full = {k: np.ascontiguousarray(gold[k].T) for k in fields}
-    extra = {k: v for k, v in (("circle", pylbm.Circle), ("parallelogram", pylbm.Parallelogram))
-             if k in build.__code__.co_varnames}
+    extra = {k: v for k, v in (("circle", pylbm.Circle), ("parallelogram", pylbm.Parallelogram),
+                               ("sphere", pylbm.Sphere)) if k in build.__code__.co_varnames}
     sim = pylbm.Simulation(build(bc=pylbm.bc, generator="cython", **extra))
     demo_cases.run_to(sim, final_time)
     mask = fluid_mask(sim)

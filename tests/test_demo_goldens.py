@@ -14,14 +14,24 @@ from conftest import golden
 from oracle import OracleSimulation
 
 
+def fluid_mask(sim, stored):
+    """The fixture's fluid mask, or (large fixtures) the simulation's own,
+    checked against the fixture's reduced copy of it."""
+    if stored.ndim:
+        return stored
+    dom = sim.domain
+    inner = tuple(slice(int(h), -int(h)) for h in dom.halo)
+    mask = dom.in_or_out[inner] == dom.valin
+    assert bool(stored) == bool(mask.all())
+    return mask
+
+
 def conserved_fields(sim, moments, fields, mask):
+    mask = fluid_mask(sim, mask)
     out = {}
     for key, cons in fields.items():
         v = np.array(moments[sim.scheme.consm[sp.Symbol(cons)]], dtype=np.float64)
-        if mask.ndim:
-            v[~mask] = 0.0
-        else:
-            assert bool(mask)  # reduced fixtures: every node is fluid
+        v[~mask] = 0.0
         out[key] = v
     return out
 
