@@ -30,8 +30,8 @@ from .domain import Domain
 from .scheme import Scheme
 from .simulation import from_storage, RAW_DTYPE
 
-TILE_BLOCKS = (64, 128, 256)
-TILE_ROWS = (1, 2, 4, 8)
+TILE_BLOCKS = (32, 64, 128, 256)
+TILE_ROWS = (1, 2, 4, 8, 16)
 GRID_PER_SM = (0, 4, 8, 16)   # 0: one block per tile
 
 

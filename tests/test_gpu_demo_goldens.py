@@ -70,4 +70,21 @@ def test_batched_boundary_launch_equals_per_method(name):
         sim.free()
     assert np.array_equal(out[0], out[1])
     if name == "karman_vortex_street":
-        assert batched  # wall, inflow, outflow and disc lists are independent
+        # the outflow's corner links read wall ghosts the Bouzidi method writes:
+        # the methods must run one after the other
+        assert not batched
+
+
+def test_batched_boundary_launch_disc_flow():
+    """Disc, inflow and outflow of the channel periodic in y: one launch, same result."""
+    from pylbm_gb300 import workloads as W
+    d = W.cylinder(nx=192, ny=64, radius=8, center=(48, 33), re=80.0)
+    out = []
+    for batch in (True, False):
+        sim = Simulation(d, dtype="float32")
+        sim.batch_boundary = batch
+        sim.run(30)
+        out.append(np.array([sim.m[k] for k in range(sim.scheme.nv)]))
+        assert sim._bc_batch is not None
+        sim.free()
+    assert np.array_equal(out[0], out[1])
