@@ -45,6 +45,7 @@ class ExprPrinter:
 
     def __init__(self, names):
         self.names = names
+        self.products = {}  # shared-product symbol -> its product (see _cse)
 
     def __call__(self, e):
         return self.p(sp.sympify(e))
@@ -117,16 +118,20 @@ class ExprPrinter:
         return not den and len(num) >= 2
 
     def _fusable(self, a):
-        """A term c*x, x*y*..., or x^n that folds into a multiply-add."""
+        """A term c*x, x*y*..., x^n, or a shared product, that folds into a multiply-add."""
         coef, rest = a.as_coeff_Mul()
         if coef.is_Number and coef not in (1, -1) and rest != 1:
             return True
+        if rest in self.products:
+            return self._fusable(self.products[rest])
         if rest.is_Mul and self._splittable(rest):
             return True
         return bool(rest.is_Pow and rest.exp.is_Integer and rest.exp >= 2)
 
     def _fma_term(self, a, acc):
         coef, rest = a.as_coeff_Mul()
+        if coef in (1, -1) and rest in self.products:  # t + z with t = x*y: fma(x, y, z)
+            return self._fma_term(coef * self.products[rest], acc)
         if coef.is_Number and coef not in (1, -1) and rest != 1:
             return f"lbm_fma<R>({self.p(coef)}, {self.p(rest)}, {acc})"
         if rest.is_Mul:
@@ -142,26 +147,23 @@ class ExprPrinter:
         return num[0], "(" + "*".join(num[1:]) + ")"
 
 
-def _cse(exprs, prefix):
-    """Common subexpressions of sums only.
+def _cse(exprs, prefix, printer=None):
+    """Common subexpressions, with shared products known to the printer.
 
-    A shared product t = x*y would reach an addition as a plain value (t + z),
+    A shared product t = x*y reaching an addition as a plain value (t + z) is
     a pattern the compiler may or may not fuse into one multiply-add, and in
     practice fuses for packed FP32x2 operations even when both are written
-    with an explicit rounding mode.  Products are therefore substituted back
-    into the expressions, where the printer turns every product term of a sum
-    into an explicit lbm_fma, and both the scalar and the two-node kernels
-    round identically.
+    with an explicit rounding mode.  The printer is told which symbols are
+    products (``printer.products``) and writes such a term as
+    lbm_fma(x, y, z) instead, so the scalar and the two-node kernels round
+    identically; elsewhere the product is computed once.
     """
     repl, red = sp.cse(exprs, symbols=sp.numbered_symbols(prefix), optimizations="basic")
-    keep, back = [], {}
-    for sym, val in repl:
-        val = val.xreplace(back)
-        if val.is_Mul or val.is_Pow:
-            back[sym] = val
-        else:
-            keep.append((sym, sp.expand(val)))
-    return keep, [sp.expand(r.xreplace(back)) for r in red]
+    if printer is not None:
+        for sym, val in repl:
+            if val.is_Mul or val.is_Pow:
+                printer.products[sym] = val
+    return repl, red
 
 
 def _pairs(scheme):
@@ -374,9 +376,9 @@ class SchemeSource:
             else:
                 d = sp.expand(e.subs({cons[c]: dsym[c] for c in range(nc)}))
             exprs.append(d)
-        repl, red = _cse(exprs, "t_")
         lines = []
         pr = ExprPrinter(names)
+        repl, red = _cse(exprs, "t_", pr)
         for sym, val in repl:
             lines.append(f"{indent}const R {sym} = {pr(val)};")
             names[sym] = str(sym)
@@ -409,8 +411,8 @@ class SchemeSource:
         for i, s in enumerate(self.params):
             names[s] = f"prm[{i}]"
         exprs = [sc.EQ[k] for k in range(nc, sc.nv)]
-        repl, red = _cse(exprs, "u_")
         pr = ExprPrinter(names)
+        repl, red = _cse(exprs, "u_", pr)
         lines = []
         for sym, val in repl:
             lines.append(f"{indent}const R {sym} = {pr(val)};")
@@ -439,8 +441,8 @@ class SchemeSource:
 
     def _assign_block(self, targets, exprs, names, prefix, indent):
         """targets[i] = exprs[i] evaluated together (all right-hand sides first)."""
-        repl, red = _cse(exprs, f"{prefix}c_")
         pr = ExprPrinter(dict(names))
+        repl, red = _cse(exprs, f"{prefix}c_", pr)
         lines = [f"{indent}{{"]
         for sym, val in repl:
             lines.append(f"{indent}  const R {sym} = {pr(val)};")
