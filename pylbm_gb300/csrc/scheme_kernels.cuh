@@ -221,7 +221,10 @@ __device__ __forceinline__ void step_pair(const S* __restrict__ f, S* __restrict
   for (int k = 0; k < LBM_Q; ++k) Pair<S>::store(fnew + o + (long long)k * g.vstride, gv[k].v);
 }
 
-__global__ void __launch_bounds__(LBM_BLOCK) k_step_periodic_pairs(const S* __restrict__ f, S* __restrict__ fnew,
+#ifndef LBM_PAIRS_MIN_BLOCKS
+#define LBM_PAIRS_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(LBM_BLOCK, LBM_PAIRS_MIN_BLOCKS) k_step_periodic_pairs(const S* __restrict__ f, S* __restrict__ fnew,
                                                                    StepArgs a) {
   constexpr int L = LBM_DIM - 1;
   const int z = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
