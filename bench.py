@@ -320,7 +320,7 @@ def main():
     nodes = int(np.prod(grid))
     buf_bytes = sim._lat.elements * BYTES_PER_VALUE[args.dtype]
     # kernels per step: the step, plus the ghost refresh and the boundary launches
-    launches_per_step = 1 if sim.periodic else 2 + (1 if sim._bc_batch is not None else len(sim._bc_dev))
+    launches_per_step = sim.launches_per_step()
     step_kernel = ("lbm_scheme::k_step_periodic_pairs" if sim.periodic and args.dtype in ("float16", "bfloat16")
                    else "lbm_scheme::k_step_periodic" if sim.periodic else "lbm_scheme::k_step_ghost")
     for _ in range(args.warmup):

@@ -178,6 +178,12 @@ int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* 
 #define LBM_BC_NEUMANN 3
 #define LBM_BC_BOUZIDI_BOUNCE_BACK 4
 #define LBM_BC_BOUZIDI_ANTI_BOUNCE_BACK 5
+/* f[istore] = f[iload0] as stored (no conversion, no shift): the periodic
+ * ghost copies of lbm_update_halo restricted to the ghost populations that a
+ * later read observes (a pull of an interior node or a boundary load that no
+ * boundary store precedes).  Interior results equal those of the full
+ * refresh bit for bit; the other ghost populations keep stale values. */
+#define LBM_BC_GHOST_COPY 6
 
 typedef struct lbm_bc_method {
   int32_t kind;               /* LBM_BC_* */

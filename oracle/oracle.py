@@ -124,6 +124,7 @@ class OracleSimulation:
         self.t = 0.0
         self.nt = 0
         self.dt = self.domain.dx / sc.la_float
+        self.after_halo = None
         self._ready = False
 
     def extra_parameters_str(self):
@@ -173,6 +174,8 @@ class OracleSimulation:
         sc = self.scheme
         L = lib()
         L.oracle_update_halo(_p(self.f), self.dim, sc.nv, _p(self.n), _p(self.h))
+        if self.after_halo is not None:  # tests: observe the populations after the refresh
+            self.after_halo(self.f)
         for meth in self.bc.methods:
             if meth.update_feq(self):
                 meth.set_rhs()

@@ -325,3 +325,64 @@ class Boundary:
                         ilabel[meth] = np.concatenate([ilabel[meth], lab * np.ones(n, dtype=np.int64)])
                         distance[meth] = np.concatenate([distance[meth], b.distance])
         self.methods = [cls(istore[cls], ilabel[cls], distance[cls], st, value_bc, time_bc) for cls in istore]
+
+
+def observed_ghost_copies(shape_in, halo, velocities, methods):
+    """The periodic ghost copies of a step whose values something reads.
+
+    pylbm refreshes every ghost population of every axis before the boundary
+    methods (its MPI topology is periodic along all axes,
+    pylbm/domain.py:373-383, pylbm/storage.py:307-367).  On a bounded domain
+    most of those values are never read: a fluid node's pull from a ghost
+    crosses a wall, so a boundary method stores that slot first.  A ghost
+    population (k, g) is observed when
+
+    * an interior node pulls it (x - v_k = g) and no method stores it, or
+    * a method loads it and no earlier method stores it.
+
+    Returns ``(istore, iload)``, int32 link arrays ``[k, i_0, ...]`` in halo
+    coordinates with iload the periodic image of istore (the copy
+    ``lbm_update_halo`` makes), or None when an axis is shorter than its halo
+    (the periodic image is then itself a ghost and the full refresh decides).
+    """
+    n = np.asarray(shape_in, dtype=np.int64)
+    h = np.asarray(halo, dtype=np.int64)
+    dim = n.size
+    if np.any(n < h):
+        return None
+    ext = n + 2 * h
+    box = int(np.prod(ext))
+
+    def keys(lst):
+        lst = np.asarray(lst, dtype=np.int64).reshape(-1, dim + 1)
+        return lst[:, 0] * box + np.ravel_multi_index(tuple(lst[:, 1:].T), tuple(ext))
+
+    def is_ghost(lst):
+        c = np.asarray(lst, dtype=np.int64).reshape(-1, dim + 1)[:, 1:]
+        return np.any((c < h) | (c >= h + n), axis=1)
+
+    stored = np.unique(np.concatenate([keys(m.istore) for m in methods] + [np.zeros(0, np.int64)]))
+    inner = tuple(slice(int(a), int(a + b)) for a, b in zip(h, n))
+    parts = []
+    for k, v in enumerate(np.asarray(velocities, dtype=np.int64).reshape(-1, dim)):
+        if not v.any():
+            continue
+        mask = np.zeros(tuple(ext), dtype=bool)
+        mask[tuple(slice(int(a - c), int(a + b - c)) for a, b, c in zip(h, n, v))] = True
+        mask[inner] = False
+        parts.append(np.flatnonzero(mask) + k * box)
+    pulled = np.concatenate(parts) if parts else np.zeros(0, np.int64)
+    needed = [np.setdiff1d(pulled, stored)]
+    before = np.zeros(0, np.int64)
+    for m in methods:
+        for il in m.iload:
+            g = is_ghost(il)
+            needed.append(np.setdiff1d(keys(il)[g], before))
+        before = np.union1d(before, keys(m.istore))
+    needed = np.unique(np.concatenate(needed))
+    k, rem = np.divmod(needed, box)
+    c = np.array(np.unravel_index(rem, tuple(ext)), dtype=np.int64).reshape(dim, -1)
+    src = np.where(c < h[:, None], c + n[:, None], np.where(c >= (n + h)[:, None], c - n[:, None], c))
+    istore = np.ascontiguousarray(np.column_stack([k, c.T]), dtype=np.int32)
+    iload = np.ascontiguousarray(np.column_stack([k, src.T]), dtype=np.int32)
+    return istore, iload

@@ -29,7 +29,7 @@ from fractions import Fraction
 import numpy as np
 import sympy as sp
 
-from .scheme import SchemeError, to_fraction
+from .scheme import REL_U, SchemeError, to_fraction
 
 
 def _lit(x):
@@ -228,6 +228,11 @@ def _emit_combo(terms):
     return acc
 
 
+def _cheaper(a, b):
+    """The expression of the two with fewer operations (a on ties)."""
+    return b if sp.count_ops(b) < sp.count_ops(a) else a
+
+
 class SchemeSource:
     """Generated device code for one scheme and one storage form.
 
@@ -248,9 +253,13 @@ class SchemeSource:
         packed FP32x2 arithmetic where the lattice allows it.
     """
 
-    def __init__(self, scheme, shifted, c0=None, style="fast", node_pairs=True):
+    def __init__(self, scheme, shifted, c0=None, style="fast", node_pairs=True, simplify_frame=False):
         self.scheme = scheme
         self.node_pairs = bool(node_pairs)
+        # relative-velocity schemes: write the moving-frame equilibrium T(u) m_eq
+        # with u replaced by its definition and simplified (for the usual
+        # u = q / rho it reduces to constants times rho); equal up to rounding
+        self.simplify_frame = bool(simplify_frame)
         self.shifted = bool(shifted)
         if style not in ("fast", "reference"):
             raise SchemeError(f"unknown style {style!r}")
@@ -504,6 +513,9 @@ class SchemeSource:
         # relaxation of every moment with a non-zero rate towards T(u) m_eq
         eqv = sp.Matrix(sc.EQ)
         eq_rel = (sc.Tu * eqv).applyfunc(sp.expand) if rel else eqv
+        if rel and self.simplify_frame:
+            sub = {REL_U[d]: e for d, e in enumerate(sc.rel_vel)}
+            eq_rel = sp.Matrix([_cheaper(e, sp.factor(sp.cancel(e.subs(sub)))) for e in eq_rel])
         targets, exprs = [], []
         for k in range(nv):
             rate = sc.s[k]

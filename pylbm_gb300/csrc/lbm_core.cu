@@ -187,6 +187,10 @@ __global__ void __launch_bounds__(kThreads) k_boundary_batch(S* __restrict__ f, 
   int ks, k0;
   const long long os = link_slot(g, M.istore + (long long)l * w, ks);
   const long long o0 = link_slot(g, M.iload0 + (long long)l * w, k0);
+  if (M.kind == LBM_BC_GHOST_COPY) {
+    f[os] = f[o0];
+    return;
+  }
   const double f0 = (double)Store<S>::load_plain(f + o0) + a.shift[k0];
   double v;
   if (M.kind == LBM_BC_BOUZIDI_BOUNCE_BACK || M.kind == LBM_BC_BOUZIDI_ANTI_BOUNCE_BACK) {

@@ -85,7 +85,7 @@ class Ensemble:
         self._check_same_scheme()
         if c0 is None:
             c0 = [1.0] + [0.0] * (self.scheme.nconsm - 1) if self.shifted else None
-        src = SchemeSource(self.scheme, self.shifted, c0)
+        src = SchemeSource(self.scheme, self.shifted, c0, simplify_frame=self.compute == "float32")
         self.module = runtime.SchemeModule(src, dtype, self.compute)
         self._core = runtime.core()
         s = ctypes.c_void_p()

@@ -29,7 +29,7 @@ import numpy as np
 import sympy as sp
 
 from . import runtime
-from .boundary import Boundary
+from .boundary import Boundary, observed_ghost_copies
 from .codegen import SchemeSource
 from .domain import Domain
 from .scheme import Scheme
@@ -116,10 +116,18 @@ class Simulation:
         the GPU (identical to the host construction; for large obstacle
         sets); ``domain.in_or_out``/``distance``/``flag`` then stay on the
         device (``domain.download_arrays()``).
+    halo : str
+        "observed" (default): the ghost refresh copies only the ghost
+        populations that a later read observes (an interior pull or a
+        boundary load that no boundary store precedes), as extra links of the
+        boundary launch where the lists allow it; interior results are those
+        of the full refresh bit for bit, ghost populations nothing reads
+        keep stale values.  "full": pylbm's refresh of every ghost
+        population of every axis.
     """
 
     def __init__(self, dico, sorder=None, dtype="float64", check_inverse=False, initialize=True,
-                 shifted=None, parity=True, node_pairs=True, c0=None, device_domain=False):
+                 shifted=None, parity=True, node_pairs=True, c0=None, device_domain=False, halo="observed"):
         gen = str(dico.get("generator", "cuda")).upper()
         if gen != "CUDA":
             raise ValueError(f"pylbm_gb300 implements generator='cuda', not {gen!r}")
@@ -127,6 +135,9 @@ class Simulation:
             raise ValueError(f"dtype must be one of {_STORAGES}")
         self.parity = bool(parity)
         self.node_pairs = bool(node_pairs)
+        if halo not in ("observed", "full"):
+            raise ValueError("halo must be 'observed' or 'full'")
+        self.halo = halo
         self.c0 = None if c0 is None else [float(c) for c in c0]
         self.dico = dico
         self.scheme = Scheme(dico)
@@ -170,6 +181,9 @@ class Simulation:
         self._update_m = True
         self._bc_dev = []
         self._bc_batch = None
+        self._ghost = None          # observed ghost copies: (istore, iload) device lists
+        self._ghost_alone = None    # their one-entry batch table when they cannot join the methods
+        self._full_halo = True
         self.batch_boundary = True  # one launch for all boundary methods where the lists allow it
         self._graph = None
         self._graph_key = None
@@ -263,7 +277,8 @@ class Simulation:
         # relative velocity or source terms use the exact-constant form
         plain = sc.Tu is None and not sc.source_terms
         style = "reference" if (self.storage == "float64" and not self.shifted and self.parity and plain) else "fast"
-        src = SchemeSource(sc, self.shifted, c0, style=style, node_pairs=self.node_pairs)
+        src = SchemeSource(sc, self.shifted, c0, style=style, node_pairs=self.node_pairs,
+                           simplify_frame=self.compute == "float32")
         self.module = runtime.SchemeModule(src, self.storage, self.compute)
         for k in range(nv):
             self._lat.shift[k] = float(self.module.shift[k])
@@ -305,7 +320,7 @@ class Simulation:
                 raise ValueError(f"{type(meth).__name__}: link list outside the lattice")
 
     def _upload_bc(self):
-        self._bc_dev = []
+        self._free_bc()
         for meth in self.bc.methods:
             self._check_links(meth)
             dev = {"iload": [self._device_array(il, 4) for il in meth.iload],
@@ -317,7 +332,33 @@ class Simulation:
                 # copy semantics of the bounce-back: compute every link before storing
                 dev["scratch"] = runtime.DeviceBuffer(8 * max(meth.ncond, 1)) if dev["ordered"] else None
             self._bc_dev.append((meth, dev))
+        self._upload_ghost()
         self._bc_batch = self._batch_table()
+
+    def _upload_ghost(self):
+        """The ghost copies a step observes (``halo='observed'``), else the full refresh."""
+        self._full_halo = True
+        if self.halo != "observed":
+            return
+        copies = observed_ghost_copies(self.domain.shape_in, self.domain.halo,
+                                       self.scheme.stencil.get_all_velocities(), self.bc.methods)
+        if copies is None:
+            return
+        self._full_halo = False
+        istore, iload = copies
+        if len(istore):
+            self._ghost = {"istore_host": istore, "iload_host": iload, "ncond": int(len(istore)),
+                           "istore": self._device_array(istore, 4), "iload": self._device_array(iload, 4),
+                           "joined": False}
+            entry = (runtime.LBM_BC_KIND["ghost_copy"], len(istore), self._ghost["iload"].ptr, None,
+                     self._ghost["istore"].ptr, None, None)
+            self._ghost_alone = self._table([entry])
+
+    def _slot_keys(self, lst):
+        """int64 key of each [k, i_0, ...] slot of a link list."""
+        ext = [self.scheme.nv] + [n + 2 * int(h) for n, h in zip(self.domain.shape_in, self.domain.halo)]
+        lst = np.asarray(lst, dtype=np.int64).reshape(-1, len(ext))
+        return np.ravel_multi_index(tuple(lst.T), tuple(ext))
 
     @staticmethod
     def _links_independent(meth):
@@ -325,39 +366,74 @@ class Simulation:
         st = {tuple(r) for r in meth.istore.tolist()}
         return not any(tuple(r) in st for il in meth.iload for r in il.tolist())
 
-    def _batch_table(self):
-        """Device table of every method for one lbm_boundary_batch launch, or
-        None when some link of one method loads a slot another link stores
-        (then the methods run one after the other, as pylbm applies them)."""
-        if len(self._bc_dev) < 2:
-            return None
-        stores = set()
-        for meth, _ in self._bc_dev:
-            stores.update(map(tuple, meth.istore.tolist()))
-        for meth, _ in self._bc_dev:
-            if any(tuple(r) in stores for il in meth.iload for r in il.tolist()):
-                return None
-        table = (runtime.BcMethod * len(self._bc_dev))()
+    def _table(self, entries):
+        """Device lbm_bc_method table of (kind, ncond, iload0, iload1, istore, rhs, dist) entries."""
+        table = (runtime.BcMethod * len(entries))()
         first = 0
-        for i, (meth, dev) in enumerate(self._bc_dev):
-            t = table[i]
-            t.kind, t.ncond, t.first = runtime.LBM_BC_KIND[meth.kind], meth.ncond, first
-            t.iload0 = dev["iload"][0].ptr
-            t.iload1 = dev["iload"][1].ptr if len(dev["iload"]) > 1 else None
-            t.istore, t.rhs = dev["istore"].ptr, dev["rhs"].ptr
-            t.dist = dev["dist"].ptr if "dist" in dev else None
-            first += meth.ncond
+        for t, (kind, ncond, il0, il1, st, rhs, dist) in zip(table, entries):
+            t.kind, t.ncond, t.first = kind, ncond, first
+            t.iload0, t.iload1, t.istore, t.rhs, t.dist = il0, il1, st, rhs, dist
+            first += ncond
         buf = runtime.DeviceBuffer(ctypes.sizeof(table))
         runtime.check(self._core.lbm_memcpy(buf.handle, ctypes.cast(table, ctypes.c_void_p), ctypes.sizeof(table),
                                             runtime.H2D, self._stream))
         self.synchronize()
-        return buf, len(self._bc_dev), first
+        return buf, len(entries), first
+
+    def _batch_table(self):
+        """Device table of every method (and the observed ghost copies) for
+        one lbm_boundary_batch launch, or None when some load of the batch
+        reads a slot a link of the batch stores (then the ghost copies and
+        the methods run one after the other, as pylbm applies them)."""
+        entries = [(runtime.LBM_BC_KIND[meth.kind], meth.ncond, dev["iload"][0].ptr,
+                    dev["iload"][1].ptr if len(dev["iload"]) > 1 else None, dev["istore"].ptr, dev["rhs"].ptr,
+                    dev["dist"].ptr if "dist" in dev else None) for meth, dev in self._bc_dev]
+        empty = np.zeros(0, np.int64)
+        stores = np.concatenate([self._slot_keys(m.istore) for m, _ in self._bc_dev] + [empty])
+        loads = np.concatenate([self._slot_keys(il) for m, _ in self._bc_dev for il in m.iload] + [empty])
+        if np.isin(loads, stores).any():
+            return None
+        g = self._ghost
+        if g is not None and not np.isin(self._slot_keys(g["iload_host"]), stores).any():
+            # the copies read interior slots that no method stores, so they join
+            # the launch; a method load of a copied ghost slot reads the copy's
+            # source instead (the value the copy would have put there)
+            gst = self._slot_keys(g["istore_host"])
+            order = np.argsort(gst)
+            gsorted = gst[order]
+            for i, (meth, dev) in enumerate(self._bc_dev):
+                fwd, changed = [], False
+                for il in meth.iload:
+                    kk = self._slot_keys(il)
+                    pos = np.minimum(np.searchsorted(gsorted, kk), len(gsorted) - 1)
+                    hit = gsorted[pos] == kk
+                    if hit.any():
+                        il = il.copy()
+                        il[hit] = g["iload_host"][order[pos[hit]]]
+                        changed = True
+                    fwd.append(il)
+                if changed:
+                    dev["iload_fwd"] = [self._device_array(np.ascontiguousarray(a, dtype=np.int32), 4) for a in fwd]
+                    kind, ncond, _, _, st, rhs, dist = entries[i]
+                    il1 = dev["iload_fwd"][1].ptr if len(fwd) > 1 else None
+                    entries[i] = (kind, ncond, dev["iload_fwd"][0].ptr, il1, st, rhs, dist)
+            entries.insert(0, (runtime.LBM_BC_KIND["ghost_copy"], g["ncond"], g["iload"].ptr, None,
+                               g["istore"].ptr, None, None))
+            g["joined"] = True
+        if len(entries) < 2:
+            return None
+        return self._table(entries)
 
     # ------------------------------------------------------------------ step
     def _enqueue_boundary(self, F):
         lat = ctypes.byref(self._lat)
-        runtime.check(self._core.lbm_update_halo(F.handle, lat, self._stream))
-        if self._bc_batch is not None and self.batch_boundary:
+        batch = self._bc_batch is not None and self.batch_boundary
+        if self._full_halo:
+            runtime.check(self._core.lbm_update_halo(F.handle, lat, self._stream))
+        elif self._ghost is not None and not (batch and self._ghost["joined"]):
+            buf, nmeth, total = self._ghost_alone
+            runtime.check(self._core.lbm_boundary_batch(F.handle, lat, buf.handle, nmeth, total, self._stream))
+        if batch:
             buf, nmeth, total = self._bc_batch
             runtime.check(self._core.lbm_boundary_batch(F.handle, lat, buf.handle, nmeth, total, self._stream))
             return
@@ -402,6 +478,20 @@ class Simulation:
             return
         fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
         self.module.call(fn(F.handle, Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
+
+    def launches_per_step(self):
+        """Kernel launches of one step: ghost refresh, boundary methods, step."""
+        if self.periodic:
+            return 1
+        batch = self._bc_batch is not None and self.batch_boundary
+        n = 1
+        if self._full_halo or (self._ghost is not None and not (batch and self._ghost["joined"])):
+            n += 1
+        if batch:
+            return n + 1
+        for meth, dev in self._bc_dev:
+            n += 2 if meth.kind == "bouzidi_bounce_back" and dev["ordered"] else 1
+        return n
 
     def _enqueue_step(self, F, Fnew, prm):
         if not self.periodic:
@@ -588,18 +678,24 @@ class Simulation:
         for b in (self._F, self._Fnew, self._M):
             if b is not None:
                 b.free()
-        for _, dev in self._bc_dev:
-            for key, val in dev.items():
+        self._free_bc()
+        if self._stream:
+            self._core.lbm_stream_destroy(self._stream)
+            self._stream = None
+
+    def _free_bc(self):
+        for dev in [d for _, d in self._bc_dev] + ([self._ghost] if self._ghost else []):
+            for val in dev.values():
                 for b in (val if isinstance(val, list) else [val]):
                     if isinstance(b, runtime.DeviceBuffer):
                         b.free()
         self._bc_dev = []
-        if self._bc_batch is not None:
-            self._bc_batch[0].free()
-            self._bc_batch = None
-        if self._stream:
-            self._core.lbm_stream_destroy(self._stream)
-            self._stream = None
+        self._ghost = None
+        for tab in (self._bc_batch, self._ghost_alone):
+            if tab is not None:
+                tab[0].free()
+        self._bc_batch = None
+        self._ghost_alone = None
 
     def __del__(self):
         try:
