@@ -124,6 +124,14 @@ int lbm_graph_destroy(void* graph_exec);
  * (pylbm/simulation.py:374-390). */
 int lbm_update_halo(void* f, const lbm_lattice* lat, void* stream);
 
+/* One axis of that refresh, as pylbm's per-axis exchange makes it
+ * (pylbm/storage.py:331-367 one pass of the loop over d; LOOPY update_x,
+ * update_y, update_z :370-420): the two ghost slabs of `axis`, over the full
+ * extent (ghosts included) of the other axes, receive the interior layers
+ * n away along `axis` only.  Axes 0, 1, 2 in that order equal
+ * lbm_update_halo. */
+int lbm_update_halo_axis(void* f, const lbm_lattice* lat, int32_t axis, void* stream);
+
 /* Boundary-node kernels.  istore and iload0 are int32 arrays of shape
  * (ncond, dim+1): velocity index then halo coordinates, the layout pylbm
  * gives them after BoundaryMethod.fix_iload (pylbm/boundary.py:226-235).

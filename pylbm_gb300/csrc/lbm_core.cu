@@ -25,6 +25,7 @@ struct HaloPlan {
   long long slab_cells[6];
   long long slab_begin[7];
   int nslab;
+  int only;  // -1: every axis, wrapped along every axis; else this axis alone
 };
 
 __device__ __forceinline__ int wrap_index(int i, int n, int h) {
@@ -41,7 +42,7 @@ __global__ void __launch_bounds__(kThreads) k_update_halo(S* __restrict__ f, Geo
   int slab = 0;
   while (slab + 1 < p.nslab && t >= p.slab_begin[slab + 1]) ++slab;
   long long r = t - p.slab_begin[slab];
-  int axis = slab >> 1, side = slab & 1;
+  int axis = p.only >= 0 ? p.only : slab >> 1, side = slab & 1;
   int ext[3], idx[3];
   for (int d = 0; d < 3; ++d) ext[d] = g.n[d] + 2 * g.h[d];
   ext[axis] = g.h[axis];
@@ -52,7 +53,8 @@ __global__ void __launch_bounds__(kThreads) k_update_halo(S* __restrict__ f, Geo
   }
   if (side) idx[axis] += g.n[axis] + g.h[axis];
   int src[3];
-  for (int d = 0; d < 3; ++d) src[d] = (d < g.dim) ? wrap_index(idx[d], g.n[d], g.h[d]) : idx[d];
+  for (int d = 0; d < 3; ++d)
+    src[d] = (d < g.dim && (p.only < 0 || d == p.only)) ? wrap_index(idx[d], g.n[d], g.h[d]) : idx[d];
   long long o_dst = (long long)k * g.vstride + node_offset(g, idx[0], idx[1], idx[2]);
   long long o_src = (long long)k * g.vstride + node_offset(g, src[0], src[1], src[2]);
   f[o_dst] = f[o_src];
@@ -566,14 +568,17 @@ int lbm_graph_destroy(void* graph_exec) {
   return cuda_check(cudaGraphExecDestroy((cudaGraphExec_t)graph_exec), "cudaGraphExecDestroy");
 }
 
-int lbm_update_halo(void* f, const lbm_lattice* lat, void* stream) {
-  int rc = check_lattice(lat, "lbm_update_halo");
+static int update_halo(void* f, const lbm_lattice* lat, int only, void* stream, const char* who) {
+  int rc = check_lattice(lat, who);
   if (rc) return rc;
-  if (!f) return fail(LBM_ERR_ARG, "lbm_update_halo: f is NULL");
+  if (!f) return fail(LBM_ERR_ARG, "%s: f is NULL", who);
+  if (only >= lat->dim) return fail(LBM_ERR_ARG, "%s: axis %d of a %d-D lattice", who, only, lat->dim);
   HaloPlan p;
   p.nslab = 0;
+  p.only = only;
   p.slab_begin[0] = 0;
   for (int a = 0; a < lat->dim; ++a) {
+    if (only >= 0 && a != only) continue;
     long long cells = lat->halo[a];
     for (int d = 0; d < 3; ++d)
       if (d != a) cells *= (long long)(lat->n[d] + 2 * lat->halo[d]);
@@ -591,8 +596,17 @@ int lbm_update_halo(void* f, const lbm_lattice* lat, void* stream) {
   return dispatch_dtype(lat->dtype, [&](auto* tag) {
     using S = std::remove_pointer_t<decltype(tag)>;
     k_update_halo<S><<<grid, kThreads, 0, s>>>((S*)f, g, p);
-    return launch_check("lbm_update_halo");
+    return launch_check(who);
   });
+}
+
+int lbm_update_halo(void* f, const lbm_lattice* lat, void* stream) {
+  return update_halo(f, lat, -1, stream, "lbm_update_halo");
+}
+
+int lbm_update_halo_axis(void* f, const lbm_lattice* lat, int32_t axis, void* stream) {
+  if (axis < 0) return fail(LBM_ERR_ARG, "lbm_update_halo_axis: axis %d", axis);
+  return update_halo(f, lat, axis, stream, "lbm_update_halo_axis");
 }
 
 int lbm_bounce_back(void* f, const int32_t* iload0, const int32_t* istore, int32_t ncond,
