@@ -423,10 +423,17 @@ typedef struct lbm_instance {
  * instance; a tile is `rows_per_tile` rows x `span` consecutive nodes of the
  * last axis (span = block, or 2 x block with LBM_INSTANCE_PAIRS).  `parity`
  * selects which of the two buffers is read (then the other is written).
- * `grid` blocks of `block` threads stride over the tiles (grid = 0: one
- * block per tile). */
+ * `grid` blocks of `block` threads (32 to LBM_ENSEMBLE_MAX_BLOCK, a multiple
+ * of 32) stride over the tiles (grid = 0: one block per tile). */
+#define LBM_ENSEMBLE_MAX_BLOCK 256
 int lbm_ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
                       int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream);
+
+/* The same step when every instance carries LBM_INSTANCE_PAIRS (the caller
+ * checks; 16-bit storage modules only): a kernel with the two-node path
+ * alone, which needs fewer registers. */
+int lbm_ensemble_step_pairs(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
+                            int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream);
 
 #ifdef __cplusplus
 }

@@ -201,8 +201,9 @@ __device__ __forceinline__ lbm::F2 pull_pair(const S* __restrict__ p, int vl, in
 #define LBM_OUTER(vx, vy, vz) (off0[(vx) + 1] + off1[(vy) + 1])
 #endif
 
-__device__ __forceinline__ void step_pair(const S* __restrict__ f, S* __restrict__ fnew, const Geo& g,
-                                          const lbm::F2 (&prm)[kPrm], int i0, int i1, int i2, int z, int nL) {
+// the pulled values of the two nodes (z, z + 1) of a row, periodic wrap
+__device__ __forceinline__ void pull_pairs(const S* __restrict__ f, const Geo& g, int i0, int i1, int i2, int z,
+                                           int nL, lbm::F2 (&gv)[LBM_Q]) {
   const long long o = lbm::node_offset(g, i0, i1, i2);
   long long off0[3] = {0, 0, 0}, off1[3] = {0, 0, 0};
 #pragma unroll
@@ -211,16 +212,30 @@ __device__ __forceinline__ void step_pair(const S* __restrict__ f, S* __restrict
     if (LBM_DIM > 2) off1[s + 1] = wrap_off(i1, s, g.n[1], g.h[1], g.stride[1]);
   }
   (void)off1;
-  lbm::F2 gv[LBM_Q];
 #define LBM_PULL_PAIR(k, vx, vy, vz) \
   gv[k] = pull_pair(f + o + (long long)(k) * g.vstride + LBM_OUTER(vx, vy, vz), LBM_VL(vx, vy, vz), z, nL);
   LBM_FOR_EACH_V(LBM_PULL_PAIR)
 #undef LBM_PULL_PAIR
+}
+
+__device__ __forceinline__ void collide_store_pairs(S* __restrict__ fnew, const Geo& g, const lbm::F2 (&prm)[kPrm],
+                                                    int i0, int i1, int i2, lbm::F2 (&gv)[LBM_Q]) {
+  const long long o = lbm::node_offset(g, i0, i1, i2);
   lbm_collide<lbm::F2>(gv, prm);
 #pragma unroll
   for (int k = 0; k < LBM_Q; ++k) Pair<S>::store(fnew + o + (long long)k * g.vstride, gv[k].v);
 }
 
+__device__ __forceinline__ void step_pair(const S* __restrict__ f, S* __restrict__ fnew, const Geo& g,
+                                          const lbm::F2 (&prm)[kPrm], int i0, int i1, int i2, int z, int nL) {
+  lbm::F2 gv[LBM_Q];
+  pull_pairs(f, g, i0, i1, i2, z, nL, gv);
+  collide_store_pairs(fnew, g, prm, i0, i1, i2, gv);
+}
+
+#ifndef LBM_ENSEMBLE_ROW_PAIRS
+#define LBM_ENSEMBLE_ROW_PAIRS 1
+#endif
 #ifndef LBM_PAIRS_MIN_BLOCKS
 #define LBM_PAIRS_MIN_BLOCKS 1
 #endif
@@ -258,10 +273,11 @@ __device__ __forceinline__ void row_coords(const Geo& g, int r, int col, int (&i
   idx[0] = idx[1] = idx[2] = 0;
   int q = r;
 #pragma unroll
-  for (int d = L - 1; d >= 0; --d) {
+  for (int d = L - 1; d >= 1; --d) {
     idx[d] = q % g.n[d] + g.h[d];
     q /= g.n[d];
   }
+  if (L >= 1) idx[0] = q + g.h[0];  // r < rows: the outermost index needs no modulo
   idx[L] = col + g.h[L];
 }
 
@@ -294,9 +310,13 @@ __device__ __forceinline__ void step_node(const S* __restrict__ f, S* __restrict
 // (span = blockDim.x, or 2 blockDim.x for LBM_INSTANCE_PAIRS, where a thread
 // updates two neighbouring nodes).  The per-node work is the periodic step
 // above with the instance's own geometry and run-time parameters.
-__global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, const lbm_instance* __restrict__ inst,
-                                                         const int* __restrict__ tile_inst, int ntiles,
-                                                         int rows_per_tile, int parity) {
+// kPairsOnly: every instance carries LBM_INSTANCE_PAIRS (the caller checks),
+// so the kernel holds the two-node path alone (fewer registers).
+template <bool kPairsOnly>
+__global__ void __launch_bounds__(LBM_ENSEMBLE_MAX_BLOCK) k_step_ensemble(S* __restrict__ arena,
+                                                                          const lbm_instance* __restrict__ inst,
+                                                                          const int* __restrict__ tile_inst,
+                                                                          int ntiles, int rows_per_tile, int parity) {
   constexpr int L = LBM_DIM - 1;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const lbm_instance* I = inst + tile_inst[tile];
@@ -331,7 +351,21 @@ __global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, c
       lbm::F2 prm2[kPrm];
 #pragma unroll
       for (int p = 0; p < kPrm; ++p) prm2[p] = lbm::F2((float)I->prm[p < LBM_MAX_PRM ? p : 0]);
-      for (int r = r0; r < r1; ++r) {
+      int r = r0;
+#if LBM_ENSEMBLE_ROW_PAIRS
+      // two rows at a time: both rows' loads are issued before either collide
+      for (; r + 1 < r1; r += 2) {
+        int a[3], b[3];
+        row_coords(g, r, z, a);
+        row_coords(g, r + 1, z, b);
+        lbm::F2 ga[LBM_Q], gb[LBM_Q];
+        pull_pairs(f, g, a[0], a[1], a[2], z, nL, ga);
+        pull_pairs(f, g, b[0], b[1], b[2], z, nL, gb);
+        collide_store_pairs(fnew, g, prm2, a[0], a[1], a[2], ga);
+        collide_store_pairs(fnew, g, prm2, b[0], b[1], b[2], gb);
+      }
+#endif
+      for (; r < r1; ++r) {
         int idx[3];
         row_coords(g, r, z, idx);
         step_pair(f, fnew, g, prm2, idx[0], idx[1], idx[2], z, nL);
@@ -339,6 +373,7 @@ __global__ void __launch_bounds__(1024) k_step_ensemble(S* __restrict__ arena, c
       continue;
     }
 #endif
+    if (kPairsOnly) continue;  // not reached: the caller checked every instance
     R prm[kPrm];
 #pragma unroll
     for (int p = 0; p < kPrm; ++p) prm[p] = (R)I->prm[p < LBM_MAX_PRM ? p : 0];
@@ -735,20 +770,39 @@ int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_latt
   return lbm::launch_check(who);
 }
 
-int lbm_ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
-                      int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream) {
+static int ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
+                         int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream,
+                         bool pairs_only, const char* who) {
   using namespace lbm_scheme;
-  if (!arena || !inst || !tile_instance) return lbm::fail(LBM_ERR_ARG, "lbm_ensemble_step: NULL argument");
-  if (ntiles < 0 || rows_per_tile < 1 || block < 32 || block > 1024 || (block % 32) || grid < 0 ||
+  if (!arena || !inst || !tile_instance) return lbm::fail(LBM_ERR_ARG, "%s: NULL argument", who);
+  if (ntiles < 0 || rows_per_tile < 1 || block < 32 || block > LBM_ENSEMBLE_MAX_BLOCK || (block % 32) || grid < 0 ||
       (parity != 0 && parity != 1))
-    return lbm::fail(LBM_ERR_ARG, "lbm_ensemble_step: ntiles=%d rows_per_tile=%d block=%d grid=%d parity=%d",
-                     ntiles, rows_per_tile, block, grid, parity);
-  if (LBM_NPRM > LBM_MAX_PRM) return lbm::fail(LBM_ERR_UNSUPPORTED, "lbm_ensemble_step: too many parameters");
+    return lbm::fail(LBM_ERR_ARG, "%s: ntiles=%d rows_per_tile=%d block=%d grid=%d parity=%d", who, ntiles,
+                     rows_per_tile, block, grid, parity);
+  if (LBM_NPRM > LBM_MAX_PRM) return lbm::fail(LBM_ERR_UNSUPPORTED, "%s: too many parameters", who);
   if (ntiles == 0) return LBM_OK;
   unsigned blocks = (unsigned)(grid > 0 ? (grid < ntiles ? grid : ntiles) : ntiles);
-  k_step_ensemble<<<blocks, block, 0, (cudaStream_t)stream>>>((S*)arena, inst, tile_instance, ntiles,
-                                                               rows_per_tile, parity);
-  return lbm::launch_check("lbm_ensemble_step");
+  if (pairs_only) {
+    if (!LBM_HAS_PAIRS) return lbm::fail(LBM_ERR_UNSUPPORTED, "%s: module without the two-node path", who);
+    k_step_ensemble<true><<<blocks, block, 0, (cudaStream_t)stream>>>((S*)arena, inst, tile_instance, ntiles,
+                                                                      rows_per_tile, parity);
+  } else {
+    k_step_ensemble<false><<<blocks, block, 0, (cudaStream_t)stream>>>((S*)arena, inst, tile_instance, ntiles,
+                                                                       rows_per_tile, parity);
+  }
+  return lbm::launch_check(who);
+}
+
+int lbm_ensemble_step(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
+                      int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream) {
+  return ensemble_step(arena, inst, tile_instance, ntiles, rows_per_tile, block, grid, parity, stream, false,
+                       "lbm_ensemble_step");
+}
+
+int lbm_ensemble_step_pairs(void* arena, const lbm_instance* inst, const int32_t* tile_instance, int32_t ntiles,
+                            int32_t rows_per_tile, int32_t block, int32_t grid, int32_t parity, void* stream) {
+  return ensemble_step(arena, inst, tile_instance, ntiles, rows_per_tile, block, grid, parity, stream, true,
+                       "lbm_ensemble_step_pairs");
 }
 
 int lbm_relaxation(double* m, const lbm_lattice* mlat, const double* prm, void* stream) {

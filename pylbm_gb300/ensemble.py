@@ -206,9 +206,12 @@ class Ensemble:
     # ------------------------------------------------------------------ steps
     def _enqueue(self, parity, tile=None):
         block, rows, grid = tile or self.tile
-        dinst, dtiles, ntiles, _ = self._table(block, rows)
-        self.module.call(self.module.lib.lbm_ensemble_step(self.arena.handle, dinst.handle, dtiles.handle, ntiles,
-                                                           rows, block, grid, parity, self._stream))
+        dinst, dtiles, ntiles, insts = self._table(block, rows)
+        # every instance on the two-node path: the kernel without the one-node path
+        pairs_only = all(I.flags & runtime.LBM_INSTANCE_PAIRS for I in insts)
+        entry = self.module.lib.lbm_ensemble_step_pairs if pairs_only else self.module.lib.lbm_ensemble_step
+        self.module.call(entry(self.arena.handle, dinst.handle, dtiles.handle, ntiles, rows, block, grid, parity,
+                               self._stream))
 
     def one_time_step(self):
         self._enqueue(self.parity)
@@ -365,3 +368,31 @@ def shear_ensemble(count=512, sides=tuple(range(64, 513, 32)), nu_range=(5e-4, 5
     dicos = [W.shear_layer(n=int(s), omega=omega, seed=int(seed * 100003 + i)) for i, s in enumerate(n)]
     params = [{"omega": W.omega_from_nu(float(v))} for v in nu]
     return Ensemble(dicos, params, dtype=dtype, tile=tile), n, nu
+
+
+def main(argv=None):
+    """Time the batched shear-layer workload: ``python -m pylbm_gb300.ensemble``."""
+    import argparse
+
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--count", type=int, default=512)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--dtype", default="float16", choices=["float64", "float32", "float16", "bfloat16"])
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args(argv)
+    ens, sides, _ = shear_ensemble(count=args.count, seed=args.seed, dtype=args.dtype)
+    ens.run(4)
+    ens.synchronize()
+    e0, e1 = runtime.Event(), runtime.Event()
+    e0.record(ens._stream)
+    ens.run(args.steps)
+    e1.record(ens._stream)
+    ms = e0.elapsed_ms(e1)
+    nodes = ens.total_nodes
+    print(json.dumps({"instances": len(sides), "nodes_per_step": nodes, "steps": args.steps, "tile": list(ens.tile),
+                      "ms_per_step": ms / args.steps, "MLUPS": nodes * args.steps / (ms / 1e3) / 1e6}))
+    ens.free()
+
+
+if __name__ == "__main__":
+    main()
