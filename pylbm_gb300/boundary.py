@@ -327,6 +327,12 @@ class Boundary:
         self.methods = [cls(istore[cls], ilabel[cls], distance[cls], st, value_bc, time_bc) for cls in istore]
 
 
+def _sorted_unique(a):
+    """Sorted distinct values of an int64 array (a sort, not a hash table)."""
+    a = np.sort(a, kind="stable")
+    return a[np.concatenate(([True], a[1:] != a[:-1]))] if a.size else a
+
+
 def observed_ghost_copies(shape_in, halo, velocities, methods):
     """The periodic ghost copies of a step whose values something reads.
 
@@ -361,25 +367,24 @@ def observed_ghost_copies(shape_in, halo, velocities, methods):
         c = np.asarray(lst, dtype=np.int64).reshape(-1, dim + 1)[:, 1:]
         return np.any((c < h) | (c >= h + n), axis=1)
 
-    stored = np.unique(np.concatenate([keys(m.istore) for m in methods] + [np.zeros(0, np.int64)]))
-    inner = tuple(slice(int(a), int(a + b)) for a, b in zip(h, n))
+    stored = _sorted_unique(np.concatenate([keys(m.istore) for m in methods] + [np.zeros(0, np.int64)]))
     parts = []
     for k, v in enumerate(np.asarray(velocities, dtype=np.int64).reshape(-1, dim)):
-        if not v.any():
-            continue
-        mask = np.zeros(tuple(ext), dtype=bool)
-        mask[tuple(slice(int(a - c), int(a + b - c)) for a, b, c in zip(h, n, v))] = True
-        mask[inner] = False
-        parts.append(np.flatnonzero(mask) + k * box)
-    pulled = np.concatenate(parts) if parts else np.zeros(0, np.int64)
-    needed = [np.setdiff1d(pulled, stored)]
+        for d in np.flatnonzero(v):
+            # interior nodes whose source x - v leaves the interior along axis d
+            box_d = [np.arange(a, a + b) for a, b in zip(h, n)]
+            box_d[d] = np.arange(h[d], h[d] + v[d]) if v[d] > 0 else np.arange(h[d] + n[d] + v[d], h[d] + n[d])
+            src = np.meshgrid(*[c - s for c, s in zip(box_d, v)], indexing="ij")
+            parts.append(k * box + np.ravel_multi_index(tuple(c.ravel() for c in src), tuple(ext)))
+    pulled = _sorted_unique(np.concatenate(parts)) if parts else np.zeros(0, np.int64)
+    needed = [np.setdiff1d(pulled, stored, assume_unique=True)]
     before = np.zeros(0, np.int64)
     for m in methods:
         for il in m.iload:
             g = is_ghost(il)
-            needed.append(np.setdiff1d(keys(il)[g], before))
-        before = np.union1d(before, keys(m.istore))
-    needed = np.unique(np.concatenate(needed))
+            needed.append(np.setdiff1d(_sorted_unique(keys(il)[g]), before, assume_unique=True))
+        before = _sorted_unique(np.concatenate([before, keys(m.istore)]))
+    needed = _sorted_unique(np.concatenate(needed))
     k, rem = np.divmod(needed, box)
     c = np.array(np.unravel_index(rem, tuple(ext)), dtype=np.int64).reshape(dim, -1)
     src = np.where(c < h[:, None], c + n[:, None], np.where(c >= (n + h)[:, None], c - n[:, None], c))

@@ -209,6 +209,7 @@ class CudaModule:
         self.vmax = [int(v) for v in np.abs(sc.stencil.get_all_velocities()).max(axis=0)]
         self.signatures = routine_signatures(sc)
         self._scratch = {}
+        self._order_cache = {}
         impl = {
             "one_time_step": self._one_time_step, "f2m": self._f2m, "m2f": self._m2f,
             "equilibrium": self._equilibrium, "relaxation": self._relaxation, "transport": self._transport,
@@ -265,10 +266,22 @@ class CudaModule:
                     raise ValueError("link list outside the lattice")
         return out
 
-    @staticmethod
-    def _ordered(istore, *loads):
-        st = {tuple(r) for r in istore.host.tolist()}
-        return int(any(tuple(r) in st for il in loads for r in il.host.tolist()))
+    def _ordered(self, istore, *loads):
+        """1 when a load of the list reads a slot the list stores (link order matters)."""
+        key = (id(istore),) + tuple(id(il) for il in loads)
+        hit = self._order_cache.get(key)
+        if hit is None or hit[0] is not istore:
+            lists = [istore.host.astype(np.int64)] + [il.host.astype(np.int64) for il in loads]
+            width = lists[0].shape[1]
+            full = [a for a in lists if a.size]
+            ext = tuple(int(e) + 1 for e in np.max([a.max(axis=0) for a in full], axis=0)) if full else (1,) * width
+
+            def flat(a):
+                return np.ravel_multi_index(tuple(a.T), ext) if a.size else np.zeros(0, np.int64)
+            stored = flat(lists[0])
+            ordered = int(any(np.isin(flat(a), stored).any() for a in lists[1:]))
+            hit = self._order_cache[key] = (istore, ordered)
+        return hit[1]
 
     # -------------------------------------------------------------- routines
     def _one_time_step(self, **kw):

@@ -360,11 +360,10 @@ class Simulation:
         lst = np.asarray(lst, dtype=np.int64).reshape(-1, len(ext))
         return np.ravel_multi_index(tuple(lst.T), tuple(ext))
 
-    @staticmethod
-    def _links_independent(meth):
+    def _links_independent(self, meth):
         """True when no link reads a slot another link of the method writes."""
-        st = {tuple(r) for r in meth.istore.tolist()}
-        return not any(tuple(r) in st for il in meth.iload for r in il.tolist())
+        st = self._slot_keys(meth.istore)
+        return not any(np.isin(self._slot_keys(il), st).any() for il in meth.iload)
 
     def _table(self, entries):
         """Device lbm_bc_method table of (kind, ncond, iload0, iload1, istore, rhs, dist) entries."""

@@ -106,6 +106,34 @@ def d3q19_dhumieres(s_nu, s_e=1.2, s_eps=1.4, s_q=1.5, s_pi=1.6, s_m=1.8):
             "equilibrium": eq, "conserved_moments": [RHO, QX, QY, QZ]}
 
 
+def cavity3d(n=128, nu=1e-3, lid=0.05, bc=None, generator="cuda"):
+    """Lid-driven cube, D3Q19 MRT: bounce-back on every wall, the top wall
+    (z = 1) moving at ``lid`` along x (the 3D analogue of ``cavity``)."""
+    bc = _bc(bc)
+    w = omega_from_nu(nu)
+    rho_o = 1.0
+
+    def bc_up(f, m, x, y, z, rho, u):
+        m[RHO] = rho
+        m[QX] = rho * u
+        m[QY] = 0.0
+        m[QZ] = 0.0
+
+    return {
+        "parameters": {LA: 1.0},
+        "box": {"x": [0.0, 1.0], "y": [0.0, 1.0], "z": [0.0, 1.0], "label": [0, 0, 0, 0, 0, 1]},
+        "space_step": 1.0 / n,
+        "scheme_velocity": LA,
+        "schemes": [d3q19_dhumieres(w)],
+        "init": {RHO: rho_o, QX: 0.0, QY: 0.0, QZ: 0.0},
+        "boundary_conditions": {
+            0: {"method": {0: bc.BounceBack}},
+            1: {"method": {0: bc.BounceBack}, "value": (bc_up, (rho_o, lid))},
+        },
+        "generator": generator,
+    }
+
+
 def tgv3d(n=256, nu=2e-3, u0=0.04, generator="cuda"):
     """Periodic Taylor-Green vortex on [0, 2pi)^3 with n^3 nodes (lattice units, la = 1)."""
     w = omega_from_nu(nu)
