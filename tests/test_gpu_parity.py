@@ -245,3 +245,18 @@ def test_relative_velocity_fp32_against_oracle(case, steps, tol, monkeypatch):
         sim.free()
     assert errs[0] < tol, errs
     assert errs[0] <= 1.5 * errs[1], errs
+
+
+@pytest.mark.parametrize("dtype,tol", [("float64", 1e-12), ("float32", 2e-5)])
+def test_lid_driven_cube_against_oracle(dtype, tol):
+    """D3Q19 cube with bounce-back on all six walls and a moving lid (the
+    bounded 3D bench workload at 16^3) against the FP64 oracle."""
+    o = OracleSimulation(W.cavity3d(n=16))
+    o.run(30)
+    ref = o.moments()
+    sim = Simulation(W.cavity3d(n=16), dtype=dtype)
+    sim.run(30)
+    got = _gpu_moments(sim)
+    assert np.isfinite(got).all()
+    err = rel_err(got[:4], ref[:4])
+    assert err.max() < tol, err
