@@ -233,11 +233,64 @@ __device__ __forceinline__ void step_pair(const S* __restrict__ f, S* __restrict
   collide_store_pairs(fnew, g, prm, i0, i1, i2, gv);
 }
 
-#ifndef LBM_ENSEMBLE_ROW_PAIRS
-#define LBM_ENSEMBLE_ROW_PAIRS 1
-#endif
 #ifndef LBM_PAIRS_MIN_BLOCKS
 #define LBM_PAIRS_MIN_BLOCKS 1
+#endif
+
+// Bounded domains: the pull reads the ghost layer (refreshed and written by
+// the boundary methods before the step), so the two sources of a pair need
+// no wrap.  For z = 0 the word at p - 2 holds (z - 2, z - 1): z - 1 is the
+// ghost, z - 2 the last element of the row before (in the buffer: every
+// interior row follows a ghost plane).  For the last pair the word at p + 2
+// holds (n, n + 1): n is the ghost, n + 1 lies in the row after.
+__device__ __forceinline__ lbm::F2 pull_pair_ghost(const S* __restrict__ p, int vl) {
+  const float2 w = Pair<S>::load(p);
+  if (vl == 0) return lbm::F2(w.x, w.y);
+  if (vl > 0) return lbm::F2(Pair<S>::load(p - 2).y, w.x);
+  return lbm::F2(w.y, Pair<S>::load(p + 2).x);
+}
+
+#if LBM_DIM == 1
+#define LBM_OUTER_GHOST(vx, vy, vz) 0LL
+#elif LBM_DIM == 2
+#define LBM_OUTER_GHOST(vx, vy, vz) (-(long long)(vx) * a.g.stride[0])
+#else
+#define LBM_OUTER_GHOST(vx, vy, vz) (-((long long)(vx) * a.g.stride[0] + (long long)(vy) * a.g.stride[1]))
+#endif
+
+__global__ void __launch_bounds__(LBM_BLOCK, LBM_PAIRS_MIN_BLOCKS) k_step_ghost_pairs(const S* __restrict__ f,
+                                                                                    S* __restrict__ fnew,
+                                                                                    StepArgs a) {
+  const int z = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int nL = a.g.n[LBM_DIM - 1];
+  if (z >= nL) return;
+  int i0, i1, i2;
+#if LBM_DIM == 1
+  i0 = z + a.g.h[0];
+  i1 = i2 = 0;
+#elif LBM_DIM == 2
+  i0 = blockIdx.y + a.g.h[0];
+  i1 = z + a.g.h[1];
+  i2 = 0;
+#else
+  i0 = blockIdx.z + a.g.h[0];
+  i1 = blockIdx.y + a.g.h[1];
+  i2 = z + a.g.h[2];
+#endif
+  lbm::F2 prm[kPrm];
+#pragma unroll
+  for (int p = 0; p < kPrm; ++p) prm[p] = lbm::F2((float)a.prm[p]);
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  lbm::F2 gv[LBM_Q];
+#define LBM_PULL_GHOST(k, vx, vy, vz) \
+  gv[k] = pull_pair_ghost(f + o + (long long)(k) * a.g.vstride + LBM_OUTER_GHOST(vx, vy, vz), LBM_VL(vx, vy, vz));
+  LBM_FOR_EACH_V(LBM_PULL_GHOST)
+#undef LBM_PULL_GHOST
+  collide_store_pairs(fnew, a.g, prm, i0, i1, i2, gv);
+}
+
+#ifndef LBM_ENSEMBLE_ROW_PAIRS
+#define LBM_ENSEMBLE_ROW_PAIRS 1
 #endif
 __global__ void __launch_bounds__(LBM_BLOCK, LBM_PAIRS_MIN_BLOCKS) k_step_periodic_pairs(const S* __restrict__ f, S* __restrict__ fnew,
                                                                    StepArgs a) {
@@ -665,9 +718,12 @@ static int step_common(const void* f, void* fnew, const lbm_lattice* lat, const 
   dim3 grid = node_grid(*lat, false);
   cudaStream_t s = (cudaStream_t)stream;
 #if LBM_HAS_PAIRS
-  if (periodic && pairs_fit(*lat, f, fnew)) {
+  if (pairs_fit(*lat, f, fnew)) {
     grid.x = (unsigned)((lat->n[LBM_DIM - 1] / 2 + LBM_BLOCK - 1) / LBM_BLOCK);
-    k_step_periodic_pairs<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a);
+    if (periodic)
+      k_step_periodic_pairs<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a);
+    else
+      k_step_ghost_pairs<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a);
     return lbm::launch_check(who);
   }
 #endif

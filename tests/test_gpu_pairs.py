@@ -65,3 +65,35 @@ def test_ensemble_pairs_equal_single_nodes():
     sim.run(31)
     assert np.array_equal(res[0][1], _moments(sim))
     sim.free()
+
+
+def _fits(sim):
+    """The host mirror of the kernels' two-node condition (pairs_fit)."""
+    lat = sim._lat
+    L = sim.dim - 1
+    return (lat.n[L] % 2 == 0 and (lat.origin + lat.halo[L]) % 2 == 0 and lat.vstride % 2 == 0
+            and all(lat.stride[d] % 2 == 0 for d in range(L)))
+
+
+@pytest.mark.parametrize("case,dtype", [("disc_flow", "float16"), ("cube", "float16"), ("cube", "bfloat16"),
+                                        ("geier_channel", "float16"), ("cavity", "bfloat16")])
+def test_bounded_pairs_equal_single_nodes(case, dtype):
+    """Bounded domains: the two-node step reads the ghost layer the boundary
+    methods wrote; results equal the one-node step bit for bit."""
+    make = {
+        "disc_flow": lambda: W.cylinder(nx=192, ny=64, radius=8, center=(48, 33), re=80.0),
+        "cube": lambda: W.cavity3d(n=32),
+        "geier_channel": lambda: W.karman(dx=1.0 / 32),
+        "cavity": lambda: W.cavity(n=64),
+    }[case]
+    out = []
+    for pairs in (True, False):
+        sim = Simulation(make(), dtype=dtype, node_pairs=pairs)
+        assert not sim.periodic
+        if pairs:
+            assert _fits(sim)
+        sim.run(25)
+        out.append(_moments(sim))
+        sim.free()
+    assert np.all(np.isfinite(out[0]))
+    assert np.array_equal(out[0], out[1])
