@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 import sympy as sp
 
+import demo_cases
 from pylbm_gb300 import Simulation
 from pylbm_gb300 import workloads as W
 from pylbm_gb300.ensemble import Ensemble
@@ -76,7 +77,8 @@ def _fits(sim):
 
 
 @pytest.mark.parametrize("case,dtype", [("disc_flow", "float16"), ("cube", "float16"), ("cube", "bfloat16"),
-                                        ("geier_channel", "float16"), ("cavity", "bfloat16")])
+                                        ("geier_channel", "float16"), ("cavity", "bfloat16"),
+                                        ("vectorial_channel", "float16"), ("euler_1d", "bfloat16")])
 def test_bounded_pairs_equal_single_nodes(case, dtype):
     """Bounded domains: the two-node step reads the ghost layer the boundary
     methods wrote; results equal the one-node step bit for bit."""
@@ -85,6 +87,9 @@ def test_bounded_pairs_equal_single_nodes(case, dtype):
         "cube": lambda: W.cavity3d(n=32),
         "geier_channel": lambda: W.karman(dx=1.0 / 32),
         "cavity": lambda: W.cavity(n=64),
+        # D2Q4 x 3 with Bouzidi walls and NeumannX; D1Q3 x 3 Euler with Neumann ends
+        "vectorial_channel": lambda: demo_cases.poiseuille_vec(),
+        "euler_1d": lambda: demo_cases.euler_1d(),
     }[case]
     out = []
     for pairs in (True, False):
