@@ -277,6 +277,15 @@ int lbm_links_count(const lbm_domain* d, const int32_t* flag, int32_t u, int32_t
 int lbm_links_fill(const lbm_domain* d, const int32_t* flag, const double* distance, int32_t u, int32_t label,
                    const int32_t* vsym, const int32_t* block_offsets, int32_t* rows, double* dist, void* stream);
 
+/* A strided box of one plane k of a lattice (populations in their storage
+ * type, or float64 moments) copied into a dense device array out, last axis
+ * fastest: out[i0][i1][i2] = plane k at interior node start + i * step
+ * (step may be negative; every selected node must be interior).  Reading a
+ * slice of sim.m or sim.F then moves only the slice to the host
+ * (pylbm/simulation.py:216-256 m / F, followed by the caller's indexing). */
+int lbm_gather(const void* f, const lbm_lattice* lat, int32_t k, const int32_t* start, const int32_t* count,
+               const int32_t* step, void* out, void* stream);
+
 /* Block average of the interior populations over factor^dim nodes into a
  * dense float64 array out[nv][n0/factor][n1/factor][n2/factor] (physical
  * values, last axis contiguous): restriction of a fine run onto a coarse

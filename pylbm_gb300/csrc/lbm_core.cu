@@ -210,6 +210,29 @@ __global__ void __launch_bounds__(kThreads) k_boundary_batch(S* __restrict__ f, 
   Store<S>::store(f + os, (decltype(Store<S>::load_plain(f)))(v - a.shift[ks]));
 }
 
+// ---------------------------------------------------------------- gather
+// One strided box of one plane (population or moment) into a dense array:
+// element (i0, i1, i2) of the box is interior node start + i * step.
+struct GatherBox {
+  int start[3], count[3], step[3];
+  long long total;
+};
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_gather(const S* __restrict__ f, Geo g, int k, GatherBox b,
+                                                     S* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.total) return;
+  long long r = t;
+  int idx[3];
+  for (int d = 2; d >= 0; --d) {
+    const int i = (int)(r % b.count[d]);
+    r /= b.count[d];
+    idx[d] = d < g.dim ? b.start[d] + i * b.step[d] + g.h[d] : 0;
+  }
+  out[t] = f[(long long)k * g.vstride + node_offset(g, idx[0], idx[1], idx[2])];
+}
+
 // ---------------------------------------------------------------- sums
 // Stage 1: block b of population k sums rows [b*rows_per_block, ...) of the
 // interior with FP64 warp shuffles; stage 2 adds the per-block partials.
@@ -693,6 +716,40 @@ int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* 
                                  int32_t ordered, void* stream) {
   return bouzidi_common(f, iload0, iload1, istore, ncond, rhs, dist, lat, nullptr, 1, ordered,
                         "lbm_bouzidi_anti_bounce_back", stream);
+}
+
+int lbm_gather(const void* f, const lbm_lattice* lat, int32_t k, const int32_t* start, const int32_t* count,
+               const int32_t* step, void* out, void* stream) {
+  int rc = check_lattice(lat, "lbm_gather");
+  if (rc) return rc;
+  if (!f || !out || !start || !count || !step) return fail(LBM_ERR_ARG, "lbm_gather: NULL argument");
+  if (k < 0 || k >= lat->nv) return fail(LBM_ERR_ARG, "lbm_gather: plane %d of %d", k, lat->nv);
+  GatherBox b;
+  b.total = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (d < lat->dim) {
+      const long long last = (long long)start[d] + (long long)(count[d] - 1) * step[d];
+      if (count[d] < 1 || start[d] < 0 || start[d] >= lat->n[d] || last < 0 || last >= lat->n[d])
+        return fail(LBM_ERR_ARG, "lbm_gather: axis %d start %d count %d step %d outside 0..%d", d, start[d],
+                    count[d], step[d], lat->n[d] - 1);
+      b.start[d] = start[d];
+      b.count[d] = count[d];
+      b.step[d] = step[d];
+    } else {
+      b.start[d] = 0;
+      b.count[d] = 1;
+      b.step[d] = 1;
+    }
+    b.total *= b.count[d];
+  }
+  Geo g = make_geo(*lat);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    k_gather<S><<<(unsigned)((b.total + kThreads - 1) / kThreads), kThreads, 0, s>>>((const S*)f, g, k, b,
+                                                                                      (S*)out);
+    return launch_check("lbm_gather");
+  });
 }
 
 int lbm_restrict(const void* f, const lbm_lattice* lat, double* out, int32_t factor, void* stream) {

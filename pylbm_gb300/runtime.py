@@ -213,6 +213,7 @@ def core():
             _sig(lib, "lbm_graph_destroy", I32, [P])
             _sig(lib, "lbm_update_halo", I32, [P, LP, P])
             _sig(lib, "lbm_update_halo_axis", I32, [P, LP, I32, P])
+            _sig(lib, "lbm_gather", I32, [P, LP, I32, P, P, P, P, P])
             _sig(lib, "lbm_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_anti_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_neumann", I32, [P, P, P, I32, LP, I32, P])

@@ -38,13 +38,19 @@ _STORAGES = ("float64", "float32", "float16", "bfloat16")
 
 
 class _ItemAccess:
-    """``sim.m[key]`` / ``sim.m[key] = value`` helper (pylbm/utils.py:26-81)."""
+    """``sim.m[key]`` / ``sim.m[key] = value`` helper (pylbm/utils.py:26-81).
 
-    def __init__(self, getter, setter=None):
+    With a box reader, ``sim.m[key, i0, i1, ...]`` (ints and slices over the
+    interior nodes) copies only the selected nodes from the device."""
+
+    def __init__(self, getter, setter=None, box=None):
         self._get = getter
         self._set = setter
+        self._box = box
 
     def __getitem__(self, key):
+        if isinstance(key, tuple) and self._box is not None:
+            return self._box(key[0], key[1:])
         return self._get(key)
 
     def __setitem__(self, key, value):
@@ -618,8 +624,60 @@ class Simulation:
 
     @property
     def m(self):
-        """Moments on the interior nodes (pylbm/simulation.py:216-224)."""
-        return _ItemAccess(lambda key: self._moment_halo(key)[self._inner()])
+        """Moments on the interior nodes (pylbm/simulation.py:216-224);
+        ``sim.m[key, i0, ...]`` reads only the selected nodes."""
+        return _ItemAccess(lambda key: self._moment_halo(key)[self._inner()], box=self._moment_box)
+
+    def _box_args(self, index):
+        """(start, count, step, squeeze axes) of interior indices (ints / slices)."""
+        n = list(self.domain.shape_in)
+        if len(index) > self.dim:
+            raise IndexError(f"{len(index)} indices for a {self.dim}-D field")
+        index = tuple(index) + (slice(None),) * (self.dim - len(index))
+        start, count, step, squeeze = [], [], [], []
+        for d, ix in enumerate(index):
+            if isinstance(ix, slice):
+                r = range(*ix.indices(n[d]))
+                if len(r) == 0:
+                    raise IndexError(f"empty selection on axis {d}")
+                start.append(r.start)
+                count.append(len(r))
+                step.append(r.step)
+            else:
+                i = int(ix)
+                if i < -n[d] or i >= n[d]:
+                    raise IndexError(f"index {i} out of range for axis {d} of size {n[d]}")
+                start.append(i % n[d])
+                count.append(1)
+                step.append(1)
+                squeeze.append(d)
+        return start, count, step, tuple(squeeze)
+
+    def _gather(self, buf, lat, plane, index, raw_dtype):
+        start, count, step, squeeze = self._box_args(index)
+        total = int(np.prod(count))
+        out = runtime.DeviceBuffer(total * np.dtype(raw_dtype).itemsize)
+        a = [np.array(v + [0] * (3 - len(v)), dtype=np.int32) for v in (start, count, step)]
+        runtime.check(self._core.lbm_gather(buf.handle, ctypes.byref(lat), int(plane),
+                                            *[x.ctypes.data_as(ctypes.c_void_p) for x in a],
+                                            out.handle, self._stream))
+        host = np.empty(total, dtype=raw_dtype)
+        out.download(host, stream=self._stream)
+        out.free()
+        return host.reshape(count).squeeze(axis=squeeze) if squeeze else host.reshape(count)
+
+    def _moment_box(self, key, index):
+        idx = self.scheme.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
+        if self._update_m:
+            self._m_cache = {}
+            self.module.call(self.module.lib.lbm_f2m(self._F.handle, ctypes.byref(self._lat), self._mbuf().handle,
+                                                     ctypes.byref(self._mlat), self._stream))
+            self._update_m = False
+        return self._gather(self._mbuf(), self._mlat, idx, index, np.float64)
+
+    def _population_box(self, k, index):
+        raw = self._gather(self._F, self._lat, int(k), index, RAW_DTYPE[self.storage])
+        return from_storage(raw, self.storage) + float(self._lat.shift[int(k)])
 
     def _population_halo(self, k):
         k = int(k)
@@ -647,7 +705,7 @@ class Simulation:
     @property
     def F(self):
         """Populations on the interior nodes (pylbm/simulation.py:248-256)."""
-        return _ItemAccess(lambda k: self._population_halo(k)[self._inner()])
+        return _ItemAccess(lambda k: self._population_halo(k)[self._inner()], box=self._population_box)
 
     # ------------------------------------------------------------------ checks
     def population_sums(self):

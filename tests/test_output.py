@@ -3,6 +3,7 @@ import os
 import sys
 
 import numpy as np
+import pytest
 
 from pylbm_gb300.output import H5File, write_h5
 
@@ -48,3 +49,21 @@ def test_reads_the_same_structure_as_pylbm_files(tmp_path):
     (name, addr), = f.group_entries(*np.frombuffer(f.entry(f.root_entry)[3], dtype="<u8"))
     assert name == "a"
     assert [m[0] for m in f.messages(addr)] == [0x0001, 0x0003, 0x0005, 0x0008, 0x0012]
+
+
+def test_box_arguments_of_interior_indices():
+    """Index normalisation behind sim.m[key, ...] (no GPU)."""
+    from pylbm_gb300.simulation import Simulation
+
+    class Fake:
+        dim = 2
+
+        class domain:
+            shape_in = [10, 6]
+    box = Simulation._box_args
+    assert box(Fake, (slice(None), 2)) == ([0, 2], [10, 1], [1, 1], (1,))
+    assert box(Fake, (slice(8, 1, -3), -1)) == ([8, 5], [3, 1], [-3, 1], (1,))
+    assert box(Fake, (3,)) == ([3, 0], [1, 6], [1, 1], (0,))
+    for bad in [(10, 0), (0, slice(4, 4)), (0, 0, 0)]:
+        with pytest.raises(IndexError):
+            box(Fake, bad)
