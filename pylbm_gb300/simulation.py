@@ -189,6 +189,8 @@ class Simulation:
         self._bc_batch = None
         self._ghost = None          # observed ghost copies: (istore, iload) device lists
         self._ghost_alone = None    # their one-entry batch table when they cannot join the methods
+        self._batch_bufs = []       # device lists made for the batch table
+        self._batch_rhs = []        # right-hand sides of derived batch entries (refreshed with time_bc)
         self._full_halo = True
         self.batch_boundary = True  # one launch for all boundary methods where the lists allow it
         self._graph = None
@@ -387,47 +389,102 @@ class Simulation:
 
     def _batch_table(self):
         """Device table of every method (and the observed ghost copies) for
-        one lbm_boundary_batch launch, or None when some load of the batch
-        reads a slot a link of the batch stores (then the ghost copies and
-        the methods run one after the other, as pylbm applies them)."""
-        entries = [(runtime.LBM_BC_KIND[meth.kind], meth.ncond, dev["iload"][0].ptr,
-                    dev["iload"][1].ptr if len(dev["iload"]) > 1 else None, dev["istore"].ptr, dev["rhs"].ptr,
-                    dev["dist"].ptr if "dist" in dev else None) for meth, dev in self._bc_dev]
-        empty = np.zeros(0, np.int64)
-        stores = np.concatenate([self._slot_keys(m.istore) for m, _ in self._bc_dev] + [empty])
-        loads = np.concatenate([self._slot_keys(il) for m, _ in self._bc_dev for il in m.iload] + [empty])
-        if np.isin(loads, stores).any():
+        one lbm_boundary_batch launch, or None when the links cannot all read
+        the populations as they are before the launch (then the ghost copies
+        and the methods run one after the other, as pylbm applies them).
+
+        Every link of a batch reads the state before the launch.  Two kinds of
+        load see a value another link writes in the sequential order, and are
+        rewritten: a load of a copied ghost slot reads the copy's source, and a
+        Neumann link whose load slot another method stores (the outflow's corner
+        links reading a wall's ghosts) takes that method's formula for the slot
+        and stores its result (the value the copy would have moved)."""
+        self._batch_rhs = []   # (device rhs of a derived entry, method index, link indices)
+        self._batch_bufs = []  # device lists made for the table
+        methods = [m for m, _ in self._bc_dev]
+        if not methods:
             return None
+        empty = np.zeros(0, np.int64)
+        st_keys = [self._slot_keys(m.istore) for m in methods]
+        stores = np.concatenate(st_keys + [empty])
+        order = np.argsort(stores, kind="stable")
+        st_sorted = stores[order]
+        if st_sorted.size and (st_sorted[1:] == st_sorted[:-1]).any():
+            return None  # a slot stored twice: the method order decides
+        owner_m = np.concatenate([np.full(len(k), i) for i, k in enumerate(st_keys)] + [empty])
+        owner_l = np.concatenate([np.arange(len(k)) for k in st_keys] + [empty])
+        entries = []
+        for i, m in enumerate(methods):
+            loads = [self._slot_keys(il) for il in m.iload]
+            hits = [np.isin(k, stores) for k in loads]
+            if not any(h.any() for h in hits):
+                entries.append({"kind": m.kind, "iload": list(m.iload), "istore": m.istore, "method": i,
+                                "links": None})
+                continue
+            if m.kind != "neumann":
+                return None
+            h = hits[0]
+            src = order[np.searchsorted(st_sorted, loads[0][h])]
+            pm, pl = owner_m[src], owner_l[src]
+            if any(methods[p].kind == "neumann" for p in np.unique(pm)):
+                return None  # a copy of a copy
+            keep = np.flatnonzero(~h)
+            if keep.size:
+                entries.append({"kind": "neumann", "iload": [m.iload[0][keep]], "istore": m.istore[keep],
+                                "method": i, "links": keep})
+            for p in np.unique(pm):
+                sel = pm == p
+                links = pl[sel]
+                entries.append({"kind": methods[p].kind, "iload": [il[links] for il in methods[p].iload],
+                                "istore": m.istore[h][sel], "method": int(p), "links": links})
         g = self._ghost
         if g is not None and not np.isin(self._slot_keys(g["iload_host"]), stores).any():
             # the copies read interior slots that no method stores, so they join
-            # the launch; a method load of a copied ghost slot reads the copy's
-            # source instead (the value the copy would have put there)
+            # the launch; a load of a copied ghost slot reads the copy's source
             gst = self._slot_keys(g["istore_host"])
-            order = np.argsort(gst)
-            gsorted = gst[order]
-            for i, (meth, dev) in enumerate(self._bc_dev):
-                fwd, changed = [], False
-                for il in meth.iload:
+            gorder = np.argsort(gst)
+            gsorted = gst[gorder]
+            for e in entries:
+                fwd = []
+                for il in e["iload"]:
                     kk = self._slot_keys(il)
                     pos = np.minimum(np.searchsorted(gsorted, kk), len(gsorted) - 1)
                     hit = gsorted[pos] == kk
                     if hit.any():
                         il = il.copy()
-                        il[hit] = g["iload_host"][order[pos[hit]]]
-                        changed = True
+                        il[hit] = g["iload_host"][gorder[pos[hit]]]
                     fwd.append(il)
-                if changed:
-                    dev["iload_fwd"] = [self._device_array(np.ascontiguousarray(a, dtype=np.int32), 4) for a in fwd]
-                    kind, ncond, _, _, st, rhs, dist = entries[i]
-                    il1 = dev["iload_fwd"][1].ptr if len(fwd) > 1 else None
-                    entries[i] = (kind, ncond, dev["iload_fwd"][0].ptr, il1, st, rhs, dist)
-            entries.insert(0, (runtime.LBM_BC_KIND["ghost_copy"], g["ncond"], g["iload"].ptr, None,
-                               g["istore"].ptr, None, None))
+                e["iload"] = fwd
             g["joined"] = True
-        if len(entries) < 2:
+        rows = []
+        if g is not None and g["joined"]:
+            rows.append((runtime.LBM_BC_KIND["ghost_copy"], g["ncond"], g["iload"].ptr, None, g["istore"].ptr,
+                         None, None))
+        for e in entries:
+            i, links = e["method"], e["links"]
+            m, dev = self._bc_dev[i]
+            if links is None and all(a is b for a, b in zip(e["iload"], m.iload)):
+                il = dev["iload"]
+                st = dev["istore"]
+            else:
+                il = [self._device_array(np.ascontiguousarray(a, dtype=np.int32), 4) for a in e["iload"]]
+                st = self._device_array(np.ascontiguousarray(e["istore"], dtype=np.int32), 4)
+                self._batch_bufs += il + [st]
+            rhs, dist = dev["rhs"], dev.get("dist")
+            if links is not None:
+                rhs = self._device_array(np.ascontiguousarray(m.rhs[links], dtype=np.float64), 8)
+                self._batch_rhs.append((rhs, i, links))
+                self._batch_bufs.append(rhs)
+                if dist is not None:
+                    dist = self._device_array(np.ascontiguousarray(np.asarray(m.s, dtype=np.float64)[links]), 8)
+                    self._batch_bufs.append(dist)
+            rows.append((runtime.LBM_BC_KIND[e["kind"]], int(len(e["istore"])), il[0].ptr,
+                         il[1].ptr if len(il) > 1 else None, st.ptr, rhs.ptr, dist.ptr if dist is not None else None))
+        if len(rows) < 2:
+            if g is not None:
+                g["joined"] = False
             return None
-        return self._table(entries)
+        return self._table(rows)
 
     # ------------------------------------------------------------------ step
     def _enqueue_boundary(self, F):
@@ -507,10 +564,13 @@ class Simulation:
         """Ghost refresh then every boundary method (pylbm/simulation.py:374-390)."""
         if self.periodic:
             return
-        for meth, dev in self._bc_dev:
+        for i, (meth, dev) in enumerate(self._bc_dev):
             if meth.update_feq(self):
                 meth.set_rhs()
                 dev["rhs"].upload(meth.rhs, stream=self._stream)
+                for buf, j, links in self._batch_rhs:
+                    if j == i:
+                        buf.upload(np.ascontiguousarray(meth.rhs[links], dtype=np.float64), stream=self._stream)
         self._enqueue_boundary(self._F)
 
     def one_time_step(self):
@@ -753,6 +813,10 @@ class Simulation:
                 tab[0].free()
         self._bc_batch = None
         self._ghost_alone = None
+        for b in self._batch_bufs:
+            b.free()
+        self._batch_bufs = []
+        self._batch_rhs = []
 
     def __del__(self):
         try:

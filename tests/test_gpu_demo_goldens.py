@@ -56,7 +56,8 @@ def test_h5_output_matches_reference_golden_file(tmp_path):
     sim.free()
 
 
-@pytest.mark.parametrize("name", ["karman_vortex_street", "poiseuille", "air_conditioning"])
+@pytest.mark.parametrize("name", ["karman_vortex_street", "poiseuille", "air_conditioning", "poiseuille_3d",
+                                  "karman_3d", "poiseuille_vec"])
 def test_batched_boundary_launch_equals_per_method(name):
     """All boundary methods in one launch give the per-method result bit for bit."""
     build, final_time, _, fields = demo_cases.CASES[name]
@@ -71,8 +72,8 @@ def test_batched_boundary_launch_equals_per_method(name):
     assert np.array_equal(out[0], out[1])
     if name == "karman_vortex_street":
         # the outflow's corner links read wall ghosts the Bouzidi method writes:
-        # the methods must run one after the other
-        assert not batched
+        # they take the Bouzidi formula of those slots inside the one launch
+        assert batched
 
 
 def test_batched_boundary_launch_disc_flow():

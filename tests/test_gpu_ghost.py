@@ -52,5 +52,5 @@ def test_disc_flow_one_boundary_launch():
 def test_walled_channel_drops_the_refresh():
     sim = Simulation(W.karman(dx=1.0 / 32), dtype="float32")
     assert sim._ghost is None and not sim._full_halo
-    assert sim.launches_per_step() == 3  # Bouzidi, outflow, step
+    assert sim.launches_per_step() == 2  # Bouzidi and outflow in one launch, then the step
     sim.free()
