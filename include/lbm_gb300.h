@@ -193,16 +193,25 @@ int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* 
  * refresh bit for bit; the other ghost populations keep stale values. */
 #define LBM_BC_GHOST_COPY 6
 
+/* Flag of lbm_bc_method.flags for FP32 / FP16 / BF16 storage: `rhs` and
+ * `dist` point to float arrays and the link computes in FP32 on the stored
+ * deviations g = f - shift: g_s = +/- g_0 + c (bounce-back, anti-bounce-back,
+ * Neumann) or g_s = ((1 - d) g_1 +/- d g_0) + c (Bouzidi), where the caller
+ * folds the shifts into c = +/- shift[k_0] + rhs - shift[k_s] (Bouzidi:
+ * (1 - d) shift[k_1] +/- d shift[k_0] + rhs - shift[k_s]) in float64 and
+ * rounds it once.  No float64 arithmetic runs on the device. */
+#define LBM_BC_FLOAT_FORM 1
+
 typedef struct lbm_bc_method {
   int32_t kind;               /* LBM_BC_* */
   int32_t ncond;
   int32_t first;              /* index of the method's first link in the batch */
-  int32_t reserved;
+  int32_t flags;              /* LBM_BC_FLOAT_FORM or 0 */
   const int32_t* iload0;
   const int32_t* iload1;      /* Bouzidi only */
   const int32_t* istore;
-  const double* rhs;          /* not for Neumann */
-  const double* dist;         /* Bouzidi only */
+  const double* rhs;          /* not for Neumann (float* with LBM_BC_FLOAT_FORM) */
+  const double* dist;         /* Bouzidi only (float* with LBM_BC_FLOAT_FORM) */
 } lbm_bc_method;
 
 int lbm_boundary_batch(void* f, const lbm_lattice* lat, const lbm_bc_method* methods, int32_t nmethods,

@@ -76,6 +76,7 @@ class DomainDesc(ctypes.Structure):
 
 LBM_BC_KIND = {"bounce_back": 1, "anti_bounce_back": 2, "neumann": 3, "bouzidi_bounce_back": 4,
                "bouzidi_anti_bounce_back": 5, "ghost_copy": 6}
+LBM_BC_FLOAT_FORM = 1
 
 
 class BcMethod(ctypes.Structure):
@@ -84,7 +85,7 @@ class BcMethod(ctypes.Structure):
         ("kind", ctypes.c_int32),
         ("ncond", ctypes.c_int32),
         ("first", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
         ("iload0", ctypes.c_void_p),
         ("iload1", ctypes.c_void_p),
         ("istore", ctypes.c_void_p),

@@ -190,7 +190,7 @@ class Simulation:
         self._ghost = None          # observed ghost copies: (istore, iload) device lists
         self._ghost_alone = None    # their one-entry batch table when they cannot join the methods
         self._batch_bufs = []       # device lists made for the batch table
-        self._batch_rhs = []        # right-hand sides of derived batch entries (refreshed with time_bc)
+        self._batch_rhs = []        # (device array, method index, host builder) of batch right-hand sides that follow time_bc
         self._full_halo = True
         self.batch_boundary = True  # one launch for all boundary methods where the lists allow it
         self._graph = None
@@ -374,11 +374,12 @@ class Simulation:
         return not any(np.isin(self._slot_keys(il), st).any() for il in meth.iload)
 
     def _table(self, entries):
-        """Device lbm_bc_method table of (kind, ncond, iload0, iload1, istore, rhs, dist) entries."""
+        """Device lbm_bc_method table of (kind, ncond, iload0, iload1, istore, rhs, dist[, flags]) entries."""
         table = (runtime.BcMethod * len(entries))()
         first = 0
-        for t, (kind, ncond, il0, il1, st, rhs, dist) in zip(table, entries):
-            t.kind, t.ncond, t.first = kind, ncond, first
+        for t, e in zip(table, entries):
+            kind, ncond, il0, il1, st, rhs, dist = e[:7]
+            t.kind, t.ncond, t.first, t.flags = kind, ncond, first, (e[7] if len(e) > 7 else 0)
             t.iload0, t.iload1, t.istore, t.rhs, t.dist = il0, il1, st, rhs, dist
             first += ncond
         buf = runtime.DeviceBuffer(ctypes.sizeof(table))
@@ -399,7 +400,7 @@ class Simulation:
         Neumann link whose load slot another method stores (the outflow's corner
         links reading a wall's ghosts) takes that method's formula for the slot
         and stores its result (the value the copy would have moved)."""
-        self._batch_rhs = []   # (device rhs of a derived entry, method index, link indices)
+        self._batch_rhs = []   # (device array, method index, host builder) refreshed with time_bc
         self._batch_bufs = []  # device lists made for the table
         methods = [m for m, _ in self._bc_dev]
         if not methods:
@@ -460,6 +461,9 @@ class Simulation:
         if g is not None and g["joined"]:
             rows.append((runtime.LBM_BC_KIND["ghost_copy"], g["ncond"], g["iload"].ptr, None, g["istore"].ptr,
                          None, None))
+        # shifted storage: the links compute in FP32 on the stored deviations,
+        # with the shifts folded into one per-link constant (LBM_BC_FLOAT_FORM)
+        float_form = self.storage != "float64"
         for e in entries:
             i, links = e["method"], e["links"]
             m, dev = self._bc_dev[i]
@@ -470,21 +474,53 @@ class Simulation:
                 il = [self._device_array(np.ascontiguousarray(a, dtype=np.int32), 4) for a in e["iload"]]
                 st = self._device_array(np.ascontiguousarray(e["istore"], dtype=np.int32), 4)
                 self._batch_bufs += il + [st]
-            rhs, dist = dev["rhs"], dev.get("dist")
-            if links is not None:
-                rhs = self._device_array(np.ascontiguousarray(m.rhs[links], dtype=np.float64), 8)
-                self._batch_rhs.append((rhs, i, links))
+            sel = slice(None) if links is None else links
+            dist_host = np.asarray(m.s, dtype=np.float64)[sel] if hasattr(m, "s") else None
+            if float_form:
+                def rhs_of(meth, e=e, sel=sel, d=dist_host):
+                    return self._float_constants(e["kind"], e["iload"], e["istore"], np.asarray(meth.rhs)[sel], d)
+                rhs = self._device_array(rhs_of(m), 4)
+                self._batch_rhs.append((rhs, i, rhs_of))
                 self._batch_bufs.append(rhs)
-                if dist is not None:
-                    dist = self._device_array(np.ascontiguousarray(np.asarray(m.s, dtype=np.float64)[links]), 8)
+                dist = None
+                if dist_host is not None:
+                    dist = self._device_array(np.ascontiguousarray(dist_host, dtype=np.float32), 4)
                     self._batch_bufs.append(dist)
+            else:
+                rhs, dist = dev["rhs"], dev.get("dist")
+                if links is not None:
+                    def rhs_of(meth, sel=sel):
+                        return np.ascontiguousarray(np.asarray(meth.rhs)[sel], dtype=np.float64)
+                    rhs = self._device_array(rhs_of(m), 8)
+                    self._batch_rhs.append((rhs, i, rhs_of))
+                    self._batch_bufs.append(rhs)
+                    if dist is not None:
+                        dist = self._device_array(np.ascontiguousarray(dist_host), 8)
+                        self._batch_bufs.append(dist)
             rows.append((runtime.LBM_BC_KIND[e["kind"]], int(len(e["istore"])), il[0].ptr,
-                         il[1].ptr if len(il) > 1 else None, st.ptr, rhs.ptr, dist.ptr if dist is not None else None))
-        if len(rows) < 2:
+                         il[1].ptr if len(il) > 1 else None, st.ptr, rhs.ptr, dist.ptr if dist is not None else None,
+                         runtime.LBM_BC_FLOAT_FORM if float_form else 0))
+        if len(rows) < (1 if float_form else 2):
             if g is not None:
                 g["joined"] = False
             return None
         return self._table(rows)
+
+    def _float_constants(self, kind, iload, istore, rhs, dist):
+        """Per-link FP32 constant of LBM_BC_FLOAT_FORM: the shifts of the load
+        and store populations folded into the right-hand side, in float64,
+        rounded once."""
+        shift = np.asarray(self.module.shift, dtype=np.float64)
+        s0 = shift[np.asarray(iload[0])[:, 0]]
+        ss = shift[np.asarray(istore)[:, 0]]
+        rhs = np.zeros(len(ss)) if kind == "neumann" else np.asarray(rhs, dtype=np.float64)
+        if kind.startswith("bouzidi"):
+            s1 = shift[np.asarray(iload[1])[:, 0]]
+            t0 = dist * s0
+            c = (1.0 - dist) * s1 + (-t0 if kind == "bouzidi_anti_bounce_back" else t0)
+        else:
+            c = -s0 if kind == "anti_bounce_back" else s0
+        return np.ascontiguousarray(c + rhs - ss, dtype=np.float32)
 
     # ------------------------------------------------------------------ step
     def _enqueue_boundary(self, F):
@@ -568,9 +604,9 @@ class Simulation:
             if meth.update_feq(self):
                 meth.set_rhs()
                 dev["rhs"].upload(meth.rhs, stream=self._stream)
-                for buf, j, links in self._batch_rhs:
+                for buf, j, rhs_of in self._batch_rhs:
                     if j == i:
-                        buf.upload(np.ascontiguousarray(meth.rhs[links], dtype=np.float64), stream=self._stream)
+                        buf.upload(rhs_of(meth), stream=self._stream)
         self._enqueue_boundary(self._F)
 
     def one_time_step(self):
