@@ -180,6 +180,7 @@ def variants(args):
          2048 * 1024, 9, 4, 500),
         # bounded 3D: bounce-back on all six walls (1.96 M links per step), moving lid
         ("cavity3d_256_f32", lambda: Simulation(W.cavity3d(n=256), dtype="float32"), 256 ** 3, 19, 4, 100),
+        ("cavity3d_256_f16", lambda: Simulation(W.cavity3d(n=256), dtype="float16"), 256 ** 3, 19, 2, 100),
     ]
     for name, make, nodes, q, es, steps in cases:
         sim = make()
