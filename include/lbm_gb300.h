@@ -201,6 +201,11 @@ int lbm_bouzidi_anti_bounce_back(void* f, const int32_t* iload0, const int32_t* 
  * (1 - d) shift[k_1] +/- d shift[k_0] + rhs - shift[k_s]) in float64 and
  * rounds it once.  No float64 arithmetic runs on the device. */
 #define LBM_BC_FLOAT_FORM 1
+/* Flag of lbm_bc_method.flags: iload0, iload1 and istore hold one int32 per
+ * link, the element offset k * vstride + node offset of the slot, instead of
+ * rows (k, i0, ...).  The population index is then unknown to the kernel,
+ * so the caller sets it with LBM_BC_FLOAT_FORM or with unshifted storage. */
+#define LBM_BC_FLAT 2
 
 typedef struct lbm_bc_method {
   int32_t kind;               /* LBM_BC_* */

@@ -186,9 +186,10 @@ __global__ void __launch_bounds__(kThreads) k_boundary_batch(S* __restrict__ f, 
   const lbm_bc_method M = a.methods[m];
   const int l = c - M.first;
   const int w = g.dim + 1;
-  int ks, k0;
-  const long long os = link_slot(g, M.istore + (long long)l * w, ks);
-  const long long o0 = link_slot(g, M.iload0 + (long long)l * w, k0);
+  const bool flat = (M.flags & LBM_BC_FLAT) != 0;
+  int ks = 0, k0 = 0;
+  const long long os = flat ? (long long)M.istore[l] : link_slot(g, M.istore + (long long)l * w, ks);
+  const long long o0 = flat ? (long long)M.iload0[l] : link_slot(g, M.iload0 + (long long)l * w, k0);
   if (M.kind == LBM_BC_GHOST_COPY) {
     f[os] = f[o0];
     return;
@@ -199,8 +200,8 @@ __global__ void __launch_bounds__(kThreads) k_boundary_batch(S* __restrict__ f, 
     const float g0 = (float)Store<S>::load_plain(f + o0);
     float v;
     if (M.kind == LBM_BC_BOUZIDI_BOUNCE_BACK || M.kind == LBM_BC_BOUZIDI_ANTI_BOUNCE_BACK) {
-      int k1;
-      const long long o1 = link_slot(g, M.iload1 + (long long)l * w, k1);
+      int k1 = 0;
+      const long long o1 = flat ? (long long)M.iload1[l] : link_slot(g, M.iload1 + (long long)l * w, k1);
       const float g1 = (float)Store<S>::load_plain(f + o1);
       const float d = reinterpret_cast<const float*>(M.dist)[l];
       const float t1 = __fmul_rn(__fsub_rn(1.0f, d), g1);
@@ -212,12 +213,13 @@ __global__ void __launch_bounds__(kThreads) k_boundary_batch(S* __restrict__ f, 
     Store<S>::store(f + os, (decltype(Store<S>::load_plain(f)))v);
     return;
   }
-  const double f0 = (double)Store<S>::load_plain(f + o0) + a.shift[k0];
+  // flat offsets carry no population index: the caller sets them for unshifted storage only
+  const double f0 = (double)Store<S>::load_plain(f + o0) + (flat ? 0.0 : a.shift[k0]);
   double v;
   if (M.kind == LBM_BC_BOUZIDI_BOUNCE_BACK || M.kind == LBM_BC_BOUZIDI_ANTI_BOUNCE_BACK) {
-    int k1;
-    const long long o1 = link_slot(g, M.iload1 + (long long)l * w, k1);
-    const double f1 = (double)Store<S>::load_plain(f + o1) + a.shift[k1];
+    int k1 = 0;
+    const long long o1 = flat ? (long long)M.iload1[l] : link_slot(g, M.iload1 + (long long)l * w, k1);
+    const double f1 = (double)Store<S>::load_plain(f + o1) + (flat ? 0.0 : a.shift[k1]);
     const double d = M.dist[l];
     const double t1 = __dmul_rn(__dsub_rn(1.0, d), f1);
     const double t0 = __dmul_rn(d, f0);
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(kThreads) k_boundary_batch(S* __restrict__ f, 
     const double sign = M.kind == LBM_BC_ANTI_BOUNCE_BACK ? -1.0 : 1.0;
     v = sign * f0 + (M.kind == LBM_BC_NEUMANN ? 0.0 : M.rhs[l]);
   }
-  Store<S>::store(f + os, (decltype(Store<S>::load_plain(f)))(v - a.shift[ks]));
+  Store<S>::store(f + os, (decltype(Store<S>::load_plain(f)))(v - (flat ? 0.0 : a.shift[ks])));
 }
 
 // ---------------------------------------------------------------- gather

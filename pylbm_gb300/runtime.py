@@ -77,6 +77,7 @@ class DomainDesc(ctypes.Structure):
 LBM_BC_KIND = {"bounce_back": 1, "anti_bounce_back": 2, "neumann": 3, "bouzidi_bounce_back": 4,
                "bouzidi_anti_bounce_back": 5, "ghost_copy": 6}
 LBM_BC_FLOAT_FORM = 1
+LBM_BC_FLAT = 2
 
 
 class BcMethod(ctypes.Structure):

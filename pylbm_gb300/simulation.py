@@ -458,16 +458,30 @@ class Simulation:
                 e["iload"] = fwd
             g["joined"] = True
         rows = []
-        if g is not None and g["joined"]:
-            rows.append((runtime.LBM_BC_KIND["ghost_copy"], g["ncond"], g["iload"].ptr, None, g["istore"].ptr,
-                         None, None))
         # shifted storage: the links compute in FP32 on the stored deviations,
         # with the shifts folded into one per-link constant (LBM_BC_FLOAT_FORM)
         float_form = self.storage != "float64"
+        # one int32 element offset per slot instead of a (k, i0, ...) row when
+        # the kernel needs no population index (LBM_BC_FLAT)
+        unshifted = not any(self._lat.shift[k] for k in range(self.scheme.nv))
+        flat = (float_form or unshifted) and self._lat.elements < 2 ** 31
+        flags = (runtime.LBM_BC_FLOAT_FORM if float_form else 0) | (runtime.LBM_BC_FLAT if flat else 0)
+        if g is not None and g["joined"]:
+            if flat:
+                gl, gs = (self._device_array(self._flat_slots(a), 4) for a in (g["iload_host"], g["istore_host"]))
+                self._batch_bufs += [gl, gs]
+            else:
+                gl, gs = g["iload"], g["istore"]
+            rows.append((runtime.LBM_BC_KIND["ghost_copy"], g["ncond"], gl.ptr, None, gs.ptr, None, None,
+                         runtime.LBM_BC_FLAT if flat else 0))
         for e in entries:
             i, links = e["method"], e["links"]
             m, dev = self._bc_dev[i]
-            if links is None and all(a is b for a, b in zip(e["iload"], m.iload)):
+            if flat:
+                il = [self._device_array(self._flat_slots(a), 4) for a in e["iload"]]
+                st = self._device_array(self._flat_slots(e["istore"]), 4)
+                self._batch_bufs += il + [st]
+            elif links is None and all(a is b for a, b in zip(e["iload"], m.iload)):
                 il = dev["iload"]
                 st = dev["istore"]
             else:
@@ -499,12 +513,21 @@ class Simulation:
                         self._batch_bufs.append(dist)
             rows.append((runtime.LBM_BC_KIND[e["kind"]], int(len(e["istore"])), il[0].ptr,
                          il[1].ptr if len(il) > 1 else None, st.ptr, rhs.ptr, dist.ptr if dist is not None else None,
-                         runtime.LBM_BC_FLOAT_FORM if float_form else 0))
+                         flags))
         if len(rows) < (1 if float_form else 2):
             if g is not None:
                 g["joined"] = False
             return None
         return self._table(rows)
+
+    def _flat_slots(self, rows):
+        """int32 element offsets k * vstride + node offset of (k, i0, ...) rows."""
+        lat = self._lat
+        rows = np.asarray(rows, dtype=np.int64).reshape(-1, self.dim + 1)
+        off = rows[:, 0] * lat.vstride + lat.origin
+        for d in range(self.dim):
+            off = off + rows[:, 1 + d] * lat.stride[d]
+        return np.ascontiguousarray(off, dtype=np.int32)
 
     def _float_constants(self, kind, iload, istore, rhs, dist):
         """Per-link FP32 constant of LBM_BC_FLOAT_FORM: the shifts of the load
