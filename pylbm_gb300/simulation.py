@@ -621,7 +621,12 @@ class Simulation:
 
     def boundary_condition(self):
         """Ghost refresh then every boundary method (pylbm/simulation.py:374-390)."""
+        if self._need_init:
+            self._initialize()
         if self.periodic:
+            # the periodic step wraps inside the interior; the ghost layer is
+            # refreshed here for the phase-by-phase routines (transport)
+            runtime.check(self._core.lbm_update_halo(self._F.handle, ctypes.byref(self._lat), self._stream))
             return
         for i, (meth, dev) in enumerate(self._bc_dev):
             if meth.update_feq(self):
@@ -638,12 +643,77 @@ class Simulation:
             self._initialize()
         self._update_m = True
         self._m_cache = {}
-        self.boundary_condition()
+        if not self.periodic:
+            self.boundary_condition()
         prm = self._prm()
         self._launch_step(self._F, self._Fnew, prm.ctypes.data_as(ctypes.c_void_p))
         self._F, self._Fnew = self._Fnew, self._F
         self.t += self.dt
         self.nt += 1
+
+    # ---------------------------------------------------- phase by phase
+    # pylbm's routines for users who split the step themselves
+    # (pylbm/simulation.py:258-372): each runs one C-ABI kernel on the
+    # device populations F / Fnew and the float64 moment array m.
+    def initialization(self):
+        """Populations from the dictionary's initial values (pylbm/simulation.py:258-320)."""
+        self._initialize()
+        self.t = 0.0
+        self.nt = 0
+
+    def _moments_ready(self):
+        if self._need_init:
+            self._initialize()
+        self._m_cache = {}
+
+    def transport(self):
+        """Fnew = pulled F, ghost layer included as it is (pylbm/simulation.py:322-327)."""
+        self._moments_ready()
+        self.module.call(self.module.lib.lbm_transport(self._F.handle, self._Fnew.handle, ctypes.byref(self._lat),
+                                                       self._stream))
+
+    def f2m(self):
+        """m = M F on the whole box (pylbm/simulation.py:344-350)."""
+        self._moments_ready()
+        self.module.call(self.module.lib.lbm_f2m(self._F.handle, ctypes.byref(self._lat), self._mbuf().handle,
+                                                 ctypes.byref(self._mlat), self._stream))
+        self._update_m = False
+
+    def m2f(self):
+        """F = M^-1 m on the whole box (pylbm/simulation.py:352-358)."""
+        self._moments_ready()
+        if self._update_m:
+            self.f2m()
+        self.module.call(self.module.lib.lbm_m2f(self._mbuf().handle, ctypes.byref(self._mlat), self._F.handle,
+                                                 ctypes.byref(self._lat), self._stream))
+
+    def equilibrium(self):
+        """Non-conserved moments of m set to their equilibrium values (pylbm/simulation.py:360-372)."""
+        self._moments_ready()
+        if self._update_m:
+            self.f2m()
+        prm = self._prm(for_init=True)
+        self.module.call(self.module.lib.lbm_equilibrium(self._mbuf().handle, ctypes.byref(self._mlat),
+                                                         prm.ctypes.data_as(ctypes.c_void_p), self._stream))
+
+    def relaxation(self):
+        """m relaxed toward the equilibrium at the scheme's rates (pylbm/simulation.py:329-334)."""
+        self._moments_ready()
+        if self._update_m:
+            self.f2m()
+        prm = self._prm()
+        self.module.call(self.module.lib.lbm_relaxation(self._mbuf().handle, ctypes.byref(self._mlat),
+                                                        prm.ctypes.data_as(ctypes.c_void_p), self._stream))
+
+    def _set_moment_halo(self, key, value):
+        idx = self.scheme.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
+        cur = self._moment_halo(idx)
+        cur[...] = value
+        plane = np.zeros(self._mlat.vstride, dtype=np.float64)
+        self._plane_view(plane, self._mlat)[...] = cur
+        self._mbuf().upload(plane, offset=idx * self._mlat.vstride * 8, stream=self._stream)
+        self._m_cache[idx] = cur
+        self._update_m = False
 
     def _drop_graph(self):
         if self._graph is not None:
@@ -739,7 +809,9 @@ class Simulation:
 
     @property
     def m_halo(self):
-        return _ItemAccess(self._moment_halo)
+        """Moments on the whole box; assignment writes the device moment array
+        (pylbm/simulation.py:200-213), which m2f turns into populations."""
+        return _ItemAccess(self._moment_halo, self._set_moment_halo)
 
     @property
     def m(self):
