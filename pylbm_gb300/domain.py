@@ -107,6 +107,22 @@ class Domain:
     def shape_in(self):
         return [int(c.size) for c in self.coords]
 
+    # coordinate accessors of pylbm's Domain (pylbm/domain.py:318-361, 444-461)
+    x = property(lambda self: self.coords[0], doc="x coordinates of the interior nodes")
+    y = property(lambda self: self.coords[1], doc="y coordinates of the interior nodes")
+    z = property(lambda self: self.coords[2], doc="z coordinates of the interior nodes")
+    x_halo = property(lambda self: self.coords_halo[0], doc="x coordinates, ghost layers included")
+    y_halo = property(lambda self: self.coords_halo[1], doc="y coordinates, ghost layers included")
+    z_halo = property(lambda self: self.coords_halo[2], doc="z coordinates, ghost layers included")
+
+    def get_bounds(self):
+        """First and last interior coordinates per axis."""
+        return (np.asarray([c[0] for c in self.coords]), np.asarray([c[-1] for c in self.coords]))
+
+    def get_bounds_halo(self):
+        """First and last coordinates per axis, ghost layers included."""
+        return (np.asarray([c[0] for c in self.coords_halo]), np.asarray([c[-1] for c in self.coords_halo]))
+
     def list_of_labels(self):
         labs = np.unique(self.box_label)
         elabs = [l for e in self.elements for l in e.label]

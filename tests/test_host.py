@@ -250,3 +250,17 @@ def test_periodic_domain_without_flags():
     assert [c.tolist() for c in dom.coords_halo] == [c.tolist() for c in full.coords_halo]
     with pytest.raises(ValueError):
         Domain(W.cavity(n=8), with_flags=False)
+
+
+def test_domain_coordinate_accessors():
+    """pylbm's Domain.x / y / z, *_halo and get_bounds (pylbm/domain.py:318-361, 444-461)."""
+    from pylbm_gb300.domain import Domain
+    d = W.cavity(n=8)
+    sc = Scheme(d)
+    dom = Domain(d, sc.stencil)
+    assert np.array_equal(dom.x, dom.coords[0]) and np.array_equal(dom.y_halo, dom.coords_halo[1])
+    assert dom.x.size == 8 and dom.x_halo.size == 10
+    lo, hi = dom.get_bounds()
+    assert np.allclose(lo, [1 / 16, 1 / 16]) and np.allclose(hi, [15 / 16, 15 / 16])
+    lo, hi = dom.get_bounds_halo()
+    assert np.allclose(lo, [-1 / 16, -1 / 16]) and np.allclose(hi, [17 / 16, 17 / 16])
