@@ -6,14 +6,17 @@ behind pylbm's ``Simulation(dico)`` / ``one_time_step()`` / ``m[...]`` API.
 The C ABI of the kernels is declared in include/lbm_gb300.h.
 """
 from . import boundary as bc
-from .boundary import AntiBounceBack, BounceBack, Neumann, NeumannX, NeumannY, NeumannZ
+from .boundary import (AntiBounceBack, BounceBack, BouzidiAntiBounceBack, BouzidiBounceBack, Neumann, NeumannX,
+                       NeumannY, NeumannZ)
 from .domain import Domain
-from .geometry import Circle
+from .geometry import Circle, Parallelogram, Sphere
+from .output import H5File
 from .scheme import Scheme, SchemeError
 from .simulation import Simulation
 from .stencil import Stencil
 
 __version__ = "0.1.0"
 
-__all__ = ["Simulation", "Scheme", "SchemeError", "Domain", "Stencil", "Circle", "bc", "BounceBack",
-           "AntiBounceBack", "Neumann", "NeumannX", "NeumannY", "NeumannZ"]
+__all__ = ["Simulation", "Scheme", "SchemeError", "Domain", "Stencil", "Circle", "Parallelogram", "Sphere",
+           "H5File", "bc", "BounceBack", "AntiBounceBack", "BouzidiBounceBack", "BouzidiAntiBounceBack", "Neumann",
+           "NeumannX", "NeumannY", "NeumannZ"]

@@ -107,6 +107,9 @@ class Domain:
     def shape_in(self):
         return [int(c.size) for c in self.coords]
 
+    # one process owns the whole domain: the demos pass this to H5File, which ignores it
+    mpi_topo = None
+
     # coordinate accessors of pylbm's Domain (pylbm/domain.py:318-361, 444-461)
     x = property(lambda self: self.coords[0], doc="x coordinates of the interior nodes")
     y = property(lambda self: self.coords[1], doc="y coordinates of the interior nodes")
