@@ -422,8 +422,8 @@ def end_to_end(sim, args, nodes):
         ev[1].record(sim._stream)
         sim.run(args.steps)
         ev[2].record(sim._stream)
-        sim.module.call(sim.module.lib.lbm_f2m(sim._F.handle, ctypes.byref(sim._lat), sim._mbuf().handle,
-                                               ctypes.byref(sim._mlat), sim._stream))
+        sim.module.call(sim.module.lib.lbm_f2m_conserved(sim._F.handle, ctypes.byref(sim._lat),
+                                                         sim._mbuf().handle, ctypes.byref(sim._mlat), sim._stream))
         runtime.check(core.lbm_memcpy(ctypes.c_void_p(out.ptr), sim._mbuf().handle, d2h, runtime.D2H,
                                       sim._stream))
         ev[3].record(sim._stream)

@@ -398,6 +398,11 @@ int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* strea
 int lbm_f2m(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat,
             void* stream);
 
+/* The conserved moments alone (planes 0 .. nconsm-1 of m; the others are left
+ * as they are): what output and conservation checks read, at a fraction of
+ * the float64 arithmetic of lbm_f2m. */
+int lbm_f2m_conserved(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat, void* stream);
+
 /* Populations from moments: f = M^-1 m (pylbm/algorithm/base.py:346-379). */
 int lbm_m2f(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat,
             void* stream);

@@ -584,6 +584,22 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_f2m(const S* __restrict__ f, doub
   for (int k = 0; k < LBM_Q; ++k) m[om + (long long)k * a.gm.vstride] = mm[k] + lbm_dev_mref[k];
 }
 
+// the conserved moments alone (what output and conservation checks read): the
+// compiler drops the algebra of the other moments
+__global__ void __launch_bounds__(LBM_BLOCK) k_f2m_conserved(const S* __restrict__ f, double* __restrict__ m,
+                                                             MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_cell(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  const long long om = lbm::node_offset(a.gm, i0, i1, i2);
+  double g[LBM_Q], mm[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) g[k] = (double)Store<S>::load(f + o + (long long)k * a.g.vstride);
+  lbm_moments<double>(g, mm);
+#pragma unroll
+  for (int k = 0; k < LBM_NCONS; ++k) m[om + (long long)k * a.gm.vstride] = mm[k] + lbm_dev_mref[k];
+}
+
 __global__ void __launch_bounds__(LBM_BLOCK) k_m2f(const double* __restrict__ m, S* __restrict__ f,
                                                    MomentArgs a) {
   int i0, i1, i2;
@@ -770,6 +786,17 @@ int lbm_f2m(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice*
   MomentArgs a = make_moment_args(lat, mlat, nullptr);
   k_f2m<<<node_grid(*lat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>((const S*)f, m, a);
   return lbm::launch_check("lbm_f2m");
+}
+
+int lbm_f2m_conserved(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_pop_lattice(lat, "lbm_f2m_conserved");
+  if (!rc) rc = check_moment_lattice(lat, mlat, "lbm_f2m_conserved");
+  if (rc) return rc;
+  if (!f || !m) return lbm::fail(LBM_ERR_ARG, "lbm_f2m_conserved: NULL buffer");
+  MomentArgs a = make_moment_args(lat, mlat, nullptr);
+  k_f2m_conserved<<<node_grid(*lat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>((const S*)f, m, a);
+  return lbm::launch_check("lbm_f2m_conserved");
 }
 
 int lbm_m2f(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat, void* stream) {

@@ -413,6 +413,7 @@ class SchemeModule:
         _sig(lib, "lbm_one_time_step_periodic", I32, [P, P, LP, P, P])
         _sig(lib, "lbm_transport", I32, [P, P, LP, P])
         _sig(lib, "lbm_f2m", I32, [P, LP, P, LP, P])
+        _sig(lib, "lbm_f2m_conserved", I32, [P, LP, P, LP, P])
         _sig(lib, "lbm_m2f", I32, [P, LP, P, LP, P])
         _sig(lib, "lbm_equilibrium", I32, [P, LP, P, P])
         _sig(lib, "lbm_relaxation", I32, [P, LP, P, P])

@@ -185,6 +185,7 @@ class Simulation:
         self.module = None
         self._m_cache = {}
         self._update_m = True
+        self._m_partial = False     # only the conserved planes of the moment array are current
         self._bc_dev = []
         self._bc_batch = None
         self._ghost = None          # observed ghost copies: (istore, iload) device lists
@@ -678,20 +679,19 @@ class Simulation:
         self.module.call(self.module.lib.lbm_f2m(self._F.handle, ctypes.byref(self._lat), self._mbuf().handle,
                                                  ctypes.byref(self._mlat), self._stream))
         self._update_m = False
+        self._m_partial = False
 
     def m2f(self):
         """F = M^-1 m on the whole box (pylbm/simulation.py:352-358)."""
         self._moments_ready()
-        if self._update_m:
-            self.f2m()
+        self._moments_for(None)
         self.module.call(self.module.lib.lbm_m2f(self._mbuf().handle, ctypes.byref(self._mlat), self._F.handle,
                                                  ctypes.byref(self._lat), self._stream))
 
     def equilibrium(self):
         """Non-conserved moments of m set to their equilibrium values (pylbm/simulation.py:360-372)."""
         self._moments_ready()
-        if self._update_m:
-            self.f2m()
+        self._moments_for(None)
         prm = self._prm(for_init=True)
         self.module.call(self.module.lib.lbm_equilibrium(self._mbuf().handle, ctypes.byref(self._mlat),
                                                          prm.ctypes.data_as(ctypes.c_void_p), self._stream))
@@ -699,14 +699,14 @@ class Simulation:
     def relaxation(self):
         """m relaxed toward the equilibrium at the scheme's rates (pylbm/simulation.py:329-334)."""
         self._moments_ready()
-        if self._update_m:
-            self.f2m()
+        self._moments_for(None)
         prm = self._prm()
         self.module.call(self.module.lib.lbm_relaxation(self._mbuf().handle, ctypes.byref(self._mlat),
                                                         prm.ctypes.data_as(ctypes.c_void_p), self._stream))
 
     def _set_moment_halo(self, key, value):
         idx = self.scheme.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
+        self._moments_for(None)  # every other plane current before this one changes
         cur = self._moment_halo(idx)
         cur[...] = value
         plane = np.zeros(self._mlat.vstride, dtype=np.float64)
@@ -762,14 +762,21 @@ class Simulation:
         runtime.check(self._core.lbm_stream_synchronize(self._stream))
 
     # ------------------------------------------------------------------ access
+    def _moments_for(self, idx):
+        """Bring the device moment array up to date for plane ``idx`` (every
+        plane when None): the conserved planes alone when only they are read."""
+        need_all = idx is None or idx >= self.scheme.nconsm
+        if self._update_m or (need_all and self._m_partial):
+            self._m_cache = {}
+            entry = self.module.lib.lbm_f2m if need_all else self.module.lib.lbm_f2m_conserved
+            self.module.call(entry(self._F.handle, ctypes.byref(self._lat), self._mbuf().handle,
+                                   ctypes.byref(self._mlat), self._stream))
+            self._update_m = False
+            self._m_partial = not need_all
+
     def _moment_halo(self, key):
         idx = self.scheme.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
-        if self._update_m:
-            self._m_cache = {}
-            mbuf = self._mbuf()
-            self.module.call(self.module.lib.lbm_f2m(self._F.handle, ctypes.byref(self._lat), mbuf.handle,
-                                                     ctypes.byref(self._mlat), self._stream))
-            self._update_m = False
+        self._moments_for(idx)
         if idx not in self._m_cache:
             # the conserved moments (what users and writers read) come in one
             # device-to-host copy; other moments one plane at a time
@@ -859,11 +866,7 @@ class Simulation:
 
     def _moment_box(self, key, index):
         idx = self.scheme.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
-        if self._update_m:
-            self._m_cache = {}
-            self.module.call(self.module.lib.lbm_f2m(self._F.handle, ctypes.byref(self._lat), self._mbuf().handle,
-                                                     ctypes.byref(self._mlat), self._stream))
-            self._update_m = False
+        self._moments_for(idx)
         return self._gather(self._mbuf(), self._mlat, idx, index, np.float64)
 
     def _population_box(self, k, index):
