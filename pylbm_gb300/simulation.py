@@ -91,6 +91,34 @@ def from_storage(raw, dtype):
 RAW_DTYPE = {"float64": np.float64, "float32": np.float32, "float16": np.float16, "bfloat16": np.uint16}
 
 
+def flat_slots(rows, lat, dim):
+    """int32 element offsets k * vstride + node offset of (k, i0, ...) rows of
+    a lattice (lbm_bc_method with LBM_BC_FLAT)."""
+    rows = np.asarray(rows, dtype=np.int64).reshape(-1, dim + 1)
+    off = rows[:, 0] * lat.vstride + lat.origin
+    for d in range(dim):
+        off = off + rows[:, 1 + d] * lat.stride[d]
+    return np.ascontiguousarray(off, dtype=np.int32)
+
+
+def float_form_constants(kind, iload, istore, rhs, dist, shift):
+    """Per-link FP32 constant of LBM_BC_FLOAT_FORM: the shifts of the load and
+    store populations folded into the right-hand side, in float64, rounded
+    once, so that the link computes on stored deviations g = f - shift:
+    g_s = +/- g_0 + c, or ((1 - d) g_1 +/- d g_0) + c for Bouzidi links."""
+    shift = np.asarray(shift, dtype=np.float64)
+    s0 = shift[np.asarray(iload[0])[:, 0]]
+    ss = shift[np.asarray(istore)[:, 0]]
+    rhs = np.zeros(len(ss)) if kind == "neumann" else np.asarray(rhs, dtype=np.float64)
+    if kind.startswith("bouzidi"):
+        s1 = shift[np.asarray(iload[1])[:, 0]]
+        t0 = dist * s0
+        c = (1.0 - dist) * s1 + (-t0 if kind == "bouzidi_anti_bounce_back" else t0)
+    else:
+        c = -s0 if kind == "anti_bounce_back" else s0
+    return np.ascontiguousarray(c + rhs - ss, dtype=np.float32)
+
+
 class Simulation:
     """A pylbm simulation whose hot path runs on the GPU.
 
@@ -522,29 +550,10 @@ class Simulation:
         return self._table(rows)
 
     def _flat_slots(self, rows):
-        """int32 element offsets k * vstride + node offset of (k, i0, ...) rows."""
-        lat = self._lat
-        rows = np.asarray(rows, dtype=np.int64).reshape(-1, self.dim + 1)
-        off = rows[:, 0] * lat.vstride + lat.origin
-        for d in range(self.dim):
-            off = off + rows[:, 1 + d] * lat.stride[d]
-        return np.ascontiguousarray(off, dtype=np.int32)
+        return flat_slots(rows, self._lat, self.dim)
 
     def _float_constants(self, kind, iload, istore, rhs, dist):
-        """Per-link FP32 constant of LBM_BC_FLOAT_FORM: the shifts of the load
-        and store populations folded into the right-hand side, in float64,
-        rounded once."""
-        shift = np.asarray(self.module.shift, dtype=np.float64)
-        s0 = shift[np.asarray(iload[0])[:, 0]]
-        ss = shift[np.asarray(istore)[:, 0]]
-        rhs = np.zeros(len(ss)) if kind == "neumann" else np.asarray(rhs, dtype=np.float64)
-        if kind.startswith("bouzidi"):
-            s1 = shift[np.asarray(iload[1])[:, 0]]
-            t0 = dist * s0
-            c = (1.0 - dist) * s1 + (-t0 if kind == "bouzidi_anti_bounce_back" else t0)
-        else:
-            c = -s0 if kind == "anti_bounce_back" else s0
-        return np.ascontiguousarray(c + rhs - ss, dtype=np.float32)
+        return float_form_constants(kind, iload, istore, rhs, dist, self.module.shift)
 
     # ------------------------------------------------------------------ step
     def _enqueue_boundary(self, F):

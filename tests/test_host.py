@@ -265,3 +265,34 @@ def test_domain_coordinate_accessors():
     assert np.allclose(lo, [1 / 16, 1 / 16]) and np.allclose(hi, [15 / 16, 15 / 16])
     lo, hi = dom.get_bounds_halo()
     assert np.allclose(lo, [-1 / 16, -1 / 16]) and np.allclose(hi, [17 / 16, 17 / 16])
+
+
+def test_float_form_constants_reproduce_the_physical_formula():
+    """LBM_BC_FLOAT_FORM: +/- g0 + c (Bouzidi: (1-d) g1 +/- d g0 + c) on stored
+    deviations equals the float64 formula on physical values minus the store shift."""
+    from pylbm_gb300.simulation import float_form_constants
+    rng = np.random.default_rng(7)
+    n, nv = 200, 9
+    shift = rng.uniform(0.02, 0.45, nv)
+    rows = lambda: np.column_stack([rng.integers(0, nv, n), rng.integers(0, 40, (n, 2))])  # noqa: E731
+    il0, il1, st = rows(), rows(), rows()
+    rhs, dist = rng.uniform(-0.1, 0.1, n), rng.uniform(0.0, 1.0, n)
+    g0, g1 = rng.uniform(-1e-3, 1e-3, n), rng.uniform(-1e-3, 1e-3, n)
+    f0, f1 = g0 + shift[il0[:, 0]], g1 + shift[il1[:, 0]]
+    for kind, sign in (("bounce_back", 1), ("anti_bounce_back", -1), ("neumann", 1)):
+        c = float_form_constants(kind, [il0], st, rhs, None, shift).astype(np.float64)
+        want = sign * f0 + (0.0 if kind == "neumann" else rhs) - shift[st[:, 0]]
+        assert np.abs(sign * g0 + c - want).max() < 1e-7
+    for kind, sign in (("bouzidi_bounce_back", 1), ("bouzidi_anti_bounce_back", -1)):
+        c = float_form_constants(kind, [il0, il1], st, rhs, dist, shift).astype(np.float64)
+        want = (1 - dist) * f1 + sign * dist * f0 + rhs - shift[st[:, 0]]
+        assert np.abs((1 - dist) * g1 + sign * dist * g0 + c - want).max() < 1e-7
+
+
+def test_flat_slots_match_the_lattice_layout():
+    from pylbm_gb300.simulation import flat_slots
+    lat = runtime.Lattice()
+    lat.vstride, lat.origin = 5000, 13
+    lat.stride[0], lat.stride[1], lat.stride[2] = 70, 1, 0
+    rows = np.array([[0, 0, 0], [2, 3, 4], [8, 41, 69]])
+    assert flat_slots(rows, lat, 2).tolist() == [13, 2 * 5000 + 13 + 3 * 70 + 4, 8 * 5000 + 13 + 41 * 70 + 69]
