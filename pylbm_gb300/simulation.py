@@ -209,6 +209,8 @@ class Simulation:
         self._stream = s
         self._F = runtime.DeviceBuffer(self._lat.elements * es)
         self._Fnew = runtime.DeviceBuffer(self._lat.elements * es)
+        for buf in (self._F, self._Fnew):  # row and plane padding stays zero (host reads whole planes)
+            buf.zero(self._stream)
         self._M = None
         self.module = None
         self._m_cache = {}
