@@ -66,3 +66,17 @@ def test_update_routines_per_axis():
     assert [n for n in sorted(sig) if n.startswith("update_")] == ["update_x", "update_y", "update_z"]
     sig1 = routine_signatures(Scheme(demo_cases.euler_1d()))
     assert [n for n in sorted(sig1) if n.startswith("update_")] == ["update_x"]
+
+
+def test_parameter_names_of_runtime_symbols():
+    """A scheme with run-time parameters: the step takes all of them, the
+    equilibrium those of m_eq, and 'lambda' is passed as 'lambda_'
+    (pylbm/algorithm/base.py:656-662)."""
+    import sympy as sp
+    omega, lam = sp.symbols("omega, lambda")
+    d = W.shear_layer(n=16, omega=omega)
+    sig = routine_signatures(Scheme(d))
+    assert "omega" in sig["one_time_step"] and "omega" in sig["relaxation"]
+    assert "omega" not in sig["equilibrium"] and "omega" not in sig["f2m"]
+    from pylbm_gb300.generator import _arg_name
+    assert _arg_name(str(lam)) == "lambda_" and _arg_name("omega") == "omega"
