@@ -112,3 +112,24 @@ def test_update_axis_is_one_periodic_pass():
     want2[:, :, 0] = want[:, :, 10]
     want2[:, :, 11] = want[:, :, 1]
     assert np.array_equal(f.get(), want2)
+
+
+def test_run_time_parameter_by_name():
+    """A periodic shear layer whose rate omega is a run-time parameter: pylbm
+    passes it to one_time_step by name; ghost refresh axis by axis, then the
+    step, equals Simulation (which wraps inside the periodic kernel) bit for bit."""
+    import sympy as sp
+    from pylbm_gb300 import workloads as W
+    omega = sp.Symbol("omega")
+    w = W.omega_from_nu(2e-3)
+    sim = Simulation(W.shear_layer(n=32, omega=omega))
+    sim.extra_parameters = {omega: w}
+    mod = CudaModule(W.shear_layer(n=32, omega=omega))
+    assert "omega" in inspect.getfullargspec(mod.one_time_step).args
+    nspace = sim.domain.shape_halo
+    f, fnew = mod.populations(nspace), mod.populations(nspace)
+    f.set(np.array([sim.F_halo[k] for k in range(9)]))
+    f, fnew = run(mod, f, fnew, [], 10, {"omega": w})
+    sim.run(10)
+    ref = np.array([sim.F[k] for k in range(9)])
+    assert np.array_equal(f.get()[:, 1:-1, 1:-1], ref)
