@@ -391,3 +391,85 @@ def observed_ghost_copies(shape_in, halo, velocities, methods):
     istore = np.ascontiguousarray(np.column_stack([k, c.T]), dtype=np.int32)
     iload = np.ascontiguousarray(np.column_stack([k, src.T]), dtype=np.int32)
     return istore, iload
+
+
+def batch_entries(methods, ext, ghost=None):
+    """The links of one lbm_boundary_batch launch, equal to the ghost copies
+    followed by the methods applied one after the other, or None.
+
+    Every link of a batch reads the populations as they are before the
+    launch.  Two kinds of load see a value another link writes in the
+    sequential order, and are rewritten: a load of a copied ghost slot reads
+    the copy's source, and a Neumann link whose load slot another
+    (non-Neumann) method stores takes that method's formula for the slot and
+    stores its result (the value the copy would have moved).  A slot stored
+    twice, a load of a slot a non-Neumann link stores or a copy of a copy
+    keep the methods sequential (None).
+
+    ``methods``: boundary methods with (ncond, dim+1) lists; ``ext``: the
+    slot extents [nv, n0 + 2 h0, ...]; ``ghost``: (istore, iload) of the
+    observed ghost copies or None.  Returns (entries, ghost_joined) with
+    entries of kind, iload (list of lists), istore, method (index whose rhs
+    and distances the entry uses) and links (indices into that method's
+    lists, None for all)."""
+    ext = tuple(int(e) for e in ext)
+
+    def keys(lst):
+        lst = np.asarray(lst, dtype=np.int64).reshape(-1, len(ext))
+        return np.ravel_multi_index(tuple(lst.T), ext)
+
+    if not methods:
+        return None
+    empty = np.zeros(0, np.int64)
+    st_keys = [keys(m.istore) for m in methods]
+    stores = np.concatenate(st_keys + [empty])
+    order = np.argsort(stores, kind="stable")
+    st_sorted = stores[order]
+    if st_sorted.size and (st_sorted[1:] == st_sorted[:-1]).any():
+        return None  # a slot stored twice: the method order decides
+    owner_m = np.concatenate([np.full(len(k), i) for i, k in enumerate(st_keys)] + [empty])
+    owner_l = np.concatenate([np.arange(len(k)) for k in st_keys] + [empty])
+    entries = []
+    for i, m in enumerate(methods):
+        loads = [keys(il) for il in m.iload]
+        hits = [np.isin(k, stores) for k in loads]
+        if not any(h.any() for h in hits):
+            entries.append({"kind": m.kind, "iload": list(m.iload), "istore": m.istore, "method": i,
+                            "links": None})
+            continue
+        if m.kind != "neumann":
+            return None
+        h = hits[0]
+        src = order[np.searchsorted(st_sorted, loads[0][h])]
+        pm, pl = owner_m[src], owner_l[src]
+        if any(methods[p].kind == "neumann" for p in np.unique(pm)):
+            return None  # a copy of a copy
+        keep = np.flatnonzero(~h)
+        if keep.size:
+            entries.append({"kind": "neumann", "iload": [m.iload[0][keep]], "istore": m.istore[keep],
+                            "method": i, "links": keep})
+        for p in np.unique(pm):
+            sel = pm == p
+            links = pl[sel]
+            entries.append({"kind": methods[p].kind, "iload": [il[links] for il in methods[p].iload],
+                            "istore": m.istore[h][sel], "method": int(p), "links": links})
+    joined = False
+    if ghost is not None and not np.isin(keys(ghost[1]), stores).any():
+        # the copies read interior slots that no method stores, so they join
+        # the launch; a load of a copied ghost slot reads the copy's source
+        gst = keys(ghost[0])
+        gorder = np.argsort(gst)
+        gsorted = gst[gorder]
+        for e in entries:
+            fwd = []
+            for il in e["iload"]:
+                kk = keys(il)
+                pos = np.minimum(np.searchsorted(gsorted, kk), len(gsorted) - 1)
+                hit = gsorted[pos] == kk
+                if hit.any():
+                    il = np.array(il, copy=True)
+                    il[hit] = ghost[1][gorder[pos[hit]]]
+                fwd.append(il)
+            e["iload"] = fwd
+        joined = True
+    return entries, joined

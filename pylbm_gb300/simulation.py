@@ -29,7 +29,7 @@ import numpy as np
 import sympy as sp
 
 from . import runtime
-from .boundary import Boundary, observed_ghost_copies
+from .boundary import Boundary, batch_entries, observed_ghost_copies
 from .codegen import SchemeSource
 from .domain import Domain
 from .scheme import Scheme
@@ -433,61 +433,15 @@ class Simulation:
         and stores its result (the value the copy would have moved)."""
         self._batch_rhs = []   # (device array, method index, host builder) refreshed with time_bc
         self._batch_bufs = []  # device lists made for the table
-        methods = [m for m, _ in self._bc_dev]
-        if not methods:
-            return None
-        empty = np.zeros(0, np.int64)
-        st_keys = [self._slot_keys(m.istore) for m in methods]
-        stores = np.concatenate(st_keys + [empty])
-        order = np.argsort(stores, kind="stable")
-        st_sorted = stores[order]
-        if st_sorted.size and (st_sorted[1:] == st_sorted[:-1]).any():
-            return None  # a slot stored twice: the method order decides
-        owner_m = np.concatenate([np.full(len(k), i) for i, k in enumerate(st_keys)] + [empty])
-        owner_l = np.concatenate([np.arange(len(k)) for k in st_keys] + [empty])
-        entries = []
-        for i, m in enumerate(methods):
-            loads = [self._slot_keys(il) for il in m.iload]
-            hits = [np.isin(k, stores) for k in loads]
-            if not any(h.any() for h in hits):
-                entries.append({"kind": m.kind, "iload": list(m.iload), "istore": m.istore, "method": i,
-                                "links": None})
-                continue
-            if m.kind != "neumann":
-                return None
-            h = hits[0]
-            src = order[np.searchsorted(st_sorted, loads[0][h])]
-            pm, pl = owner_m[src], owner_l[src]
-            if any(methods[p].kind == "neumann" for p in np.unique(pm)):
-                return None  # a copy of a copy
-            keep = np.flatnonzero(~h)
-            if keep.size:
-                entries.append({"kind": "neumann", "iload": [m.iload[0][keep]], "istore": m.istore[keep],
-                                "method": i, "links": keep})
-            for p in np.unique(pm):
-                sel = pm == p
-                links = pl[sel]
-                entries.append({"kind": methods[p].kind, "iload": [il[links] for il in methods[p].iload],
-                                "istore": m.istore[h][sel], "method": int(p), "links": links})
         g = self._ghost
-        if g is not None and not np.isin(self._slot_keys(g["iload_host"]), stores).any():
-            # the copies read interior slots that no method stores, so they join
-            # the launch; a load of a copied ghost slot reads the copy's source
-            gst = self._slot_keys(g["istore_host"])
-            gorder = np.argsort(gst)
-            gsorted = gst[gorder]
-            for e in entries:
-                fwd = []
-                for il in e["iload"]:
-                    kk = self._slot_keys(il)
-                    pos = np.minimum(np.searchsorted(gsorted, kk), len(gsorted) - 1)
-                    hit = gsorted[pos] == kk
-                    if hit.any():
-                        il = il.copy()
-                        il[hit] = g["iload_host"][gorder[pos[hit]]]
-                    fwd.append(il)
-                e["iload"] = fwd
-            g["joined"] = True
+        ghost = (g["istore_host"], g["iload_host"]) if g is not None else None
+        ext = [self.scheme.nv] + [n + 2 * int(h) for n, h in zip(self.domain.shape_in, self.domain.halo)]
+        plan = batch_entries([m for m, _ in self._bc_dev], ext, ghost)
+        if plan is None:
+            return None
+        entries, joined = plan
+        if g is not None:
+            g["joined"] = joined
         rows = []
         # shifted storage: the links compute in FP32 on the stored deviations,
         # with the shifts folded into one per-link constant (LBM_BC_FLOAT_FORM)
