@@ -296,3 +296,18 @@ def test_flat_slots_match_the_lattice_layout():
     lat.stride[0], lat.stride[1], lat.stride[2] = 70, 1, 0
     rows = np.array([[0, 0, 0], [2, 3, 4], [8, 41, 69]])
     assert flat_slots(rows, lat, 2).tolist() == [13, 2 * 5000 + 13 + 3 * 70 + 4, 8 * 5000 + 13 + 41 * 70 + 69]
+
+
+@pytest.mark.parametrize("case,storage", [("d2q13_advection", "float16"), ("d1q5_advection", "bfloat16"),
+                                          ("karman_3d", "float16"), ("riemann_p_system", "float32")])
+def test_rare_template_paths_compile(case, storage):
+    """Modules whose kernels take the less common template paths build for
+    sm_103a and load: reach 2 (no two-node path), 1D, 3D relative-velocity
+    free D3Q15 with Bouzidi links in FP16, real powers (p-system)."""
+    import demo_cases
+    sc = Scheme(demo_cases.CASES[case][0]())
+    c0 = [1.0] + [0.0] * (sc.nconsm - 1)
+    mod = runtime.SchemeModule(SchemeSource(sc, shifted=True, c0=c0, simplify_frame=True), storage, "float32")
+    for n in runtime_scheme_symbols():
+        assert hasattr(mod.lib, n), n
+    assert mod.nv == sc.nv and mod.dim == sc.dim
