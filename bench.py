@@ -48,18 +48,6 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(name):
-    """DRAM bytes per launch recorded from an ncu capture in profiles/."""
-    path = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(path):
-        return None
-    with open(path) as fh:
-        for line in fh:
-            if line.startswith("dram_bytes_per_launch_full_size:"):
-                return float(line.split(":", 1)[1].split()[0])
-    return None
-
-
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
@@ -349,8 +337,6 @@ def main():
     bpl = 2 * sim.scheme.nv * BYTES_PER_VALUE[args.dtype]
     achieved = bpl * nodes / (ms_step / 1e3) / 1e9
     peak, peak_src = measured_peaks()
-    traffic = (profiled_traffic(f"ncu_step_tgv3d_{DTYPE_TAG[args.dtype]}.md")
-               if n == 256 and args.workload == "tgv" else None)
 
     sums, bad = sim.population_sums()
     if bad:
@@ -376,7 +362,9 @@ def main():
                                "population buffers (%.3f GB each) fit in the 129 MB L2: steps are not "
                                "HBM-cold; not a roofline-grade number") % (buf_bytes / 1e9))},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
+                         "frac": achieved / peak, "traffic": None,
+                         "traffic_note": ("DRAM bytes per launch are not measurable inside this run (no profiler); "
+                                          "the ncu capture of the same kernel is summarised under profiles/"),
                          "peak_source": peak_src, "bytes_per_lup": bpl,
                          "kernel": step_kernel},
             "gpu_launches": args.steps * launches_per_step,
@@ -396,54 +384,49 @@ def main():
 def end_to_end(sim, args, nodes):
     """Same metric through the public API with host buffers.
 
-    Timed: upload of the initial populations from pinned host memory,
-    Simulation.run(K) (graph replay of the step), f2m and download of the
-    conserved moments (rho, qx, qy, qz) of the final state.
+    Timed, every run: the initial conserved moments go from page-locked host
+    memory to the device (``sim.m_halo[0:nconsm] = host``), pylbm's
+    initialisation routines turn them into populations (``sim.equilibrium()``,
+    ``sim.m2f()``), ``sim.run(K)`` advances K steps, and ``sim.fields(out=)``
+    brings the conserved moments of the final state back to page-locked host
+    memory.
     """
-    from pylbm_gb300 import runtime
+    from pylbm_gb300 import pinned_empty, runtime
 
-    core = runtime.core()
-    nbytes = sim._F.nbytes
-    pinned = runtime.PinnedBuffer(nbytes)
-    runtime.check(core.lbm_memcpy(ctypes.c_void_p(pinned.ptr), sim._F.handle, nbytes, runtime.D2H, sim._stream))
-    d2h = 8 * sim._mlat.vstride * sim.scheme.nconsm
-    out = runtime.PinnedBuffer(d2h)
-    # both host buffers are allocated and touched once before the timed region,
-    # as an application reuses its staging buffers
-    runtime.check(core.lbm_memcpy(ctypes.c_void_p(out.ptr), sim._mbuf().handle, d2h, runtime.D2H, sim._stream))
-    sim.synchronize()
+    nc = sim.scheme.nconsm
+    host_in = pinned_empty((nc,) + tuple(sim.domain.shape_halo))
+    sim.initialization()
+    for c in range(nc):  # the workload's initial conserved moments, read once, untimed
+        host_in[c] = sim.m_halo[c]
+    host_out = pinned_empty((nc,) + tuple(sim.domain.shape_in))
+    host_out[...] = 0.0  # pages touched before the timed region, as an application reuses its buffers
     reps = []
     for _ in range(8):  # the first complete run warms the copy paths and is not reported
         ev = [runtime.Event() for _ in range(4)]
         t0 = time.perf_counter()
         ev[0].record(sim._stream)
-        runtime.check(core.lbm_memcpy(sim._F.handle, ctypes.c_void_p(pinned.ptr), nbytes, runtime.H2D,
-                                      sim._stream))
+        sim.m_halo[0:nc] = host_in
+        sim.equilibrium()
+        sim.m2f()
         ev[1].record(sim._stream)
         sim.run(args.steps)
         ev[2].record(sim._stream)
-        sim.module.call(sim.module.lib.lbm_f2m_conserved(sim._F.handle, ctypes.byref(sim._lat),
-                                                         sim._mbuf().handle, ctypes.byref(sim._mlat), sim._stream))
-        runtime.check(core.lbm_memcpy(ctypes.c_void_p(out.ptr), sim._mbuf().handle, d2h, runtime.D2H,
-                                      sim._stream))
+        sim.fields(out=host_out)
         ev[3].record(sim._stream)
         sim.synchronize()
         dt = time.perf_counter() - t0
         reps.append((dt,) + tuple(ev[i].elapsed_ms(ev[i + 1]) for i in range(3)))
-    pinned.free()
-    out.free()
     reps = reps[1:]
     # the median of seven complete runs: host-memory traffic of other jobs on
     # this machine slows single copies now and then
-    dt, h2d_ms, run_ms, out_ms = sorted(reps)[len(reps) // 2]
+    dt, in_ms, run_ms, out_ms = sorted(reps)[len(reps) // 2]
     return {"value": nodes * args.steps / dt / 1e6, "unit": "MLUPS",
-            "h2d_bytes_per_step": nbytes / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-            "h2d_ms": h2d_ms, "steps_ms": run_ms, "f2m_d2h_ms": out_ms,
-            "h2d_GBs": nbytes / h2d_ms / 1e6, "d2h_GBs": d2h / out_ms / 1e6,
+            "h2d_bytes_per_step": host_in.nbytes / args.steps, "d2h_bytes_per_step": host_out.nbytes / args.steps,
+            "h2d_init_ms": in_ms, "steps_ms": run_ms, "fields_d2h_ms": out_ms,
             "runs_MLUPS": [nodes * args.steps / r[0] / 1e6 for r in reps],
-            "note": f"pinned H2D of the initial state, run({args.steps}) through the public API, "
-                    "D2H of the conserved moments; wall clock, with the stream's event split; "
-                    "median of seven complete runs after one untimed run"}
+            "note": f"public API: sim.m_halo[0:{nc}] = pinned host moments, sim.equilibrium(), sim.m2f(), "
+                    f"sim.run({args.steps}), sim.fields(out=pinned host array); wall clock, with the stream's "
+                    "event split; median of seven complete runs after one untimed run"}
 
 
 if __name__ == "__main__":

@@ -300,6 +300,28 @@ int lbm_links_fill(const lbm_domain* d, const int32_t* flag, const double* dista
 int lbm_gather(const void* f, const lbm_lattice* lat, int32_t k, const int32_t* start, const int32_t* count,
                const int32_t* step, void* out, void* stream);
 
+/* Planes first..first+count-1 of a lattice (raw stored values: populations
+ * in their storage type, or float64 moments) copied between the padded
+ * layout and a dense device array dense[plane][i0][i1][i2], last axis
+ * fastest, over the interior (with_halo = 0) or the halo-extended box
+ * (with_halo = 1); to_lattice = 1 writes the lattice from dense, 0 reads it
+ * into dense.  Assigning whole moment planes (sim.m_halo[k] = array) and
+ * reading the conserved fields then cross the host link as one contiguous
+ * copy each (pylbm/simulation.py:200-224 m_halo / m, whose numpy arrays are
+ * dense). */
+int lbm_copy_planes(void* f, const lbm_lattice* lat, int32_t first, int32_t count, int32_t with_halo,
+                    void* dense, int32_t to_lattice, void* stream);
+
+/* Measured FP64 FMA rate of the current device: eight independent DFMA
+ * chains per thread, 8 blocks of 256 threads per SM, `iters` iterations,
+ * timed with CUDA events on `stream` after one warm-up launch; writes the
+ * rate (flop/s, an FMA counting two) and the launch time.  `scratch` is
+ * device memory of lbm_fp64_fma_scratch_bytes() bytes.  The roof of the
+ * FP64 paths (the parity form of the step), which GB300's FP64 rate bounds
+ * before its HBM does.  No reference counterpart. */
+int lbm_fp64_fma_scratch_bytes(size_t* bytes);
+int lbm_fp64_fma_rate(double* scratch, int32_t iters, double* flops_per_s, float* ms, void* stream);
+
 /* Block average of the interior populations over factor^dim nodes into a
  * dense float64 array out[nv][n0/factor][n1/factor][n2/factor] (physical
  * values, last axis contiguous): restriction of a fine run onto a coarse
@@ -323,7 +345,10 @@ int lbm_population_sums(const void* f, const lbm_lattice* lat, double* sums, int
  * lbm_population_sums_noalloc_max_bytes), held by every GPU that loads the
  * library until exit.  Lattices whose partials exceed it are rejected with
  * LBM_ERR_ARG.  The first call on a device looks up the array's address for
- * that device; make it before any stream capture.  All calls share the
+ * that device; make it before any stream capture.  The address is kept with
+ * the id of the context it belongs to, so after a device reset the first
+ * call in the new context looks it up again (again before any capture).
+ * All calls share the
  * array: calls that overlap on the GPU race.  Allocates nothing.
  * No counterpart in the reference (pylbm has no conservation check). */
 int lbm_population_sums_noalloc(const void* f, const lbm_lattice* lat, double* sums,

@@ -27,7 +27,8 @@ import sysconfig
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SOURCES = "/root/reference"
+# the reference checkout: $PYLBM_REFERENCE, else a "reference" folder beside this repository
+REFERENCE_SOURCES = os.environ.get("PYLBM_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
 
 WORKLOADS = {
     # name: (workload builder, kwargs) -- the scheme decides the module; the

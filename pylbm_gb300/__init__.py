@@ -11,6 +11,7 @@ from .boundary import (AntiBounceBack, BounceBack, BouzidiAntiBounceBack, Bouzid
 from .domain import Domain
 from .geometry import Circle, Parallelogram, Sphere
 from .output import H5File
+from .runtime import pinned_empty
 from .scheme import Scheme, SchemeError
 from .simulation import Simulation
 from .stencil import Stencil
@@ -18,5 +19,5 @@ from .stencil import Stencil
 __version__ = "0.1.0"
 
 __all__ = ["Simulation", "Scheme", "SchemeError", "Domain", "Stencil", "Circle", "Parallelogram", "Sphere",
-           "H5File", "bc", "BounceBack", "AntiBounceBack", "BouzidiBounceBack", "BouzidiAntiBounceBack", "Neumann",
+           "H5File", "pinned_empty", "bc", "BounceBack", "AntiBounceBack", "BouzidiBounceBack", "BouzidiAntiBounceBack", "Neumann",
            "NeumannX", "NeumannY", "NeumannZ"]

@@ -254,6 +254,72 @@ __global__ void __launch_bounds__(kThreads) k_gather(const S* __restrict__ f, Ge
   out[t] = f[(long long)k * g.vstride + node_offset(g, idx[0], idx[1], idx[2])];
 }
 
+// ---------------------------------------------------------------- planes
+// Whole planes between the padded layout and a dense array
+// dense[plane][i0][i1][i2] over the interior or the halo-extended box, last
+// axis fastest.  One thread per element of a box row: x runs along the last
+// axis, y over the rows of the middle axis (3D) or over the first axis (2D),
+// z over planes x first-axis rows (3D).  Every thread reads and writes one
+// element, so both sides are coalesced along the row.
+struct PlaneBox {
+  int first;        // first plane of the lattice
+  int n[3];         // box extent per axis (1 beyond dim)
+  int lo[3];        // halo coordinate of the box's first node per axis
+};
+
+template <typename S, bool kToLattice>
+__global__ void __launch_bounds__(kThreads) k_planes(S* __restrict__ f, Geo g, PlaneBox b,
+                                                     S* __restrict__ dense) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = g.dim - 1;
+  if (x >= b.n[L]) return;
+  int idx[3] = {0, 0, 0};
+  long long plane, row;
+  if (g.dim == 3) {
+    const int z = blockIdx.z;
+    plane = z / b.n[0];
+    idx[0] = z - (int)plane * b.n[0];
+    idx[1] = blockIdx.y;
+    row = ((long long)plane * b.n[0] + idx[0]) * b.n[1] + idx[1];
+  } else if (g.dim == 2) {
+    plane = blockIdx.z;
+    idx[0] = blockIdx.y;
+    row = (long long)plane * b.n[0] + idx[0];
+  } else {
+    plane = blockIdx.z;
+    row = plane;
+  }
+  idx[L] = x;
+  const long long dense_at = row * b.n[L] + x;
+  const long long lat_at = (long long)(b.first + plane) * g.vstride +
+                           node_offset(g, idx[0] + b.lo[0], idx[1] + b.lo[1], idx[2] + b.lo[2]);
+  if (kToLattice)
+    f[lat_at] = dense[dense_at];
+  else
+    dense[dense_at] = f[lat_at];
+}
+
+// ---------------------------------------------------------------- FP64 rate
+// Eight independent FP64 FMA chains per thread (enough independent work to
+// cover the pipe's latency at any occupancy); the result is written so the
+// chains are not removed.  x <- x * a + b with a just below 1 stays bounded.
+constexpr int kFmaChains = 8;
+constexpr int kFmaBlocksPerSm = 8;
+
+__global__ void __launch_bounds__(kThreads) k_fp64_fma(double* __restrict__ out, int iters, double a, double b) {
+  double x[kFmaChains];
+#pragma unroll
+  for (int c = 0; c < kFmaChains; ++c) x[c] = 1e-3 * (threadIdx.x + c);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < kFmaChains; ++c) x[c] = fma(x[c], a, b);
+  }
+  double acc = 0.0;
+#pragma unroll
+  for (int c = 0; c < kFmaChains; ++c) acc += x[c];
+  out[(long long)blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
 // ---------------------------------------------------------------- sums
 // Stage 1: block b of population k sums rows [b*rows_per_block, ...) of the
 // interior with FP64 warp shuffles; stage 2 adds the per-block partials.
@@ -773,6 +839,93 @@ int lbm_gather(const void* f, const lbm_lattice* lat, int32_t k, const int32_t* 
   });
 }
 
+int lbm_copy_planes(void* f, const lbm_lattice* lat, int32_t first, int32_t count, int32_t with_halo,
+                    void* dense, int32_t to_lattice, void* stream) {
+  int rc = check_lattice(lat, "lbm_copy_planes");
+  if (rc) return rc;
+  if (!f || !dense) return fail(LBM_ERR_ARG, "lbm_copy_planes: NULL buffer");
+  if (first < 0 || count < 1 || first + count > lat->nv)
+    return fail(LBM_ERR_ARG, "lbm_copy_planes: planes %d..%d of %d", first, first + count - 1, lat->nv);
+  PlaneBox b;
+  b.first = first;
+  for (int d = 0; d < 3; ++d) {
+    b.n[d] = d < lat->dim ? lat->n[d] + (with_halo ? 2 * lat->halo[d] : 0) : 1;
+    b.lo[d] = d < lat->dim && !with_halo ? lat->halo[d] : 0;
+  }
+  const int L = lat->dim - 1;
+  // planes go in chunks whose z extent (planes x first-axis rows in 3D) fits the grid
+  const int per_plane_z = lat->dim == 3 ? b.n[0] : 1;
+  const int chunk = per_plane_z > 65535 ? 0 : 65535 / per_plane_z;
+  const unsigned gy = lat->dim == 3 ? (unsigned)b.n[1] : lat->dim == 2 ? (unsigned)b.n[0] : 1u;
+  if (chunk < 1 || gy > 65535u)
+    return fail(LBM_ERR_UNSUPPORTED, "lbm_copy_planes: box rows beyond the 65535 grid limit");
+  Geo g = make_geo(*lat);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch_dtype(lat->dtype, [&](auto* tag) {
+    using S = std::remove_pointer_t<decltype(tag)>;
+    const long long plane_elems = (long long)b.n[0] * b.n[1] * b.n[2];
+    for (int c0 = 0; c0 < count; c0 += chunk) {
+      const int c = count - c0 < chunk ? count - c0 : chunk;
+      PlaneBox bc = b;
+      bc.first = first + c0;
+      dim3 grid((unsigned)((b.n[L] + kThreads - 1) / kThreads), gy, (unsigned)(c * per_plane_z));
+      S* d = (S*)dense + (long long)c0 * plane_elems;
+      if (to_lattice)
+        k_planes<S, true><<<grid, kThreads, 0, s>>>((S*)f, g, bc, d);
+      else
+        k_planes<S, false><<<grid, kThreads, 0, s>>>((S*)f, g, bc, d);
+      int rc2 = launch_check("lbm_copy_planes");
+      if (rc2) return rc2;
+    }
+    return (int)LBM_OK;
+  });
+}
+
+int lbm_fp64_fma_scratch_bytes(size_t* bytes) {
+  int dev = 0, sms = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "lbm_fp64_fma_scratch_bytes: cudaGetDevice");
+  if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                           "lbm_fp64_fma_scratch_bytes: SM count");
+  if (rc) return rc;
+  if (!bytes) return fail(LBM_ERR_ARG, "lbm_fp64_fma_scratch_bytes: NULL");
+  *bytes = (size_t)sms * kFmaBlocksPerSm * kThreads * sizeof(double);
+  return LBM_OK;
+}
+
+int lbm_fp64_fma_rate(double* scratch, int32_t iters, double* flops_per_s, float* ms, void* stream) {
+  if (!scratch || !flops_per_s || iters < 1) return fail(LBM_ERR_ARG, "lbm_fp64_fma_rate: bad argument");
+  int dev = 0, sms = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "lbm_fp64_fma_rate: cudaGetDevice");
+  if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                           "lbm_fp64_fma_rate: SM count");
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int blocks = sms * kFmaBlocksPerSm;
+  cudaEvent_t e0, e1;
+  rc = cuda_check(cudaEventCreate(&e0), "lbm_fp64_fma_rate: event");
+  if (rc) return rc;
+  rc = cuda_check(cudaEventCreate(&e1), "lbm_fp64_fma_rate: event");
+  if (rc) {
+    cudaEventDestroy(e0);
+    return rc;
+  }
+  k_fp64_fma<<<blocks, kThreads, 0, s>>>(scratch, iters, 0.9999999, 1e-7);  // warm-up
+  cudaEventRecord(e0, s);
+  k_fp64_fma<<<blocks, kThreads, 0, s>>>(scratch, iters, 0.9999999, 1e-7);
+  cudaEventRecord(e1, s);
+  rc = launch_check("lbm_fp64_fma_rate");
+  float t = 0.f;
+  if (!rc) rc = cuda_check(cudaEventSynchronize(e1), "lbm_fp64_fma_rate: synchronize");
+  if (!rc) rc = cuda_check(cudaEventElapsedTime(&t, e0, e1), "lbm_fp64_fma_rate: elapsed");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  const double flops = 2.0 * kFmaChains * (double)iters * blocks * kThreads;
+  *flops_per_s = flops / (t * 1e-3);
+  if (ms) *ms = t;
+  return LBM_OK;
+}
+
 int lbm_restrict(const void* f, const lbm_lattice* lat, double* out, int32_t factor, void* stream) {
   int rc = check_lattice(lat, "lbm_restrict");
   if (rc) return rc;
@@ -857,7 +1010,11 @@ int lbm_population_sums(const void* f, const lbm_lattice* lat, double* sums, int
 // In host code the array's name is only a host-side stand-in, so its device
 // address is looked up once per device (cudaGetSymbolAddress, with that device
 // current) on the first call made on that device; that first call should come
-// before any stream capture.  All calls share the one array: calls that
+// before any stream capture.  The address is cached together with the unique
+// id of the context it was looked up in (cuCtxGetId): after a device reset the
+// library's module lives in a new context, the ids differ and the first call
+// in the new context looks the address up again (so that call, too, belongs
+// before any capture).  All calls share the one array: calls that
 // overlap on the GPU (e.g. on two streams) race on it.  Nothing in it needs to
 // start at zero -- every partial is written before it is read -- and the
 // non-finite counter is the caller's output, cleared by the call.
@@ -869,7 +1026,30 @@ static __device__ __align__(256) double g_noalloc_partials[kNoAllocScratchBytes 
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-void* g_noalloc_address[kMaxDevices] = {nullptr};
+struct NoAllocSlot {
+  unsigned long long context_id;  // cuCtxGetId of the context the address belongs to
+  void* address;
+};
+NoAllocSlot g_noalloc_slot[kMaxDevices] = {};
+
+// cuCtxGetId through the runtime's driver entry point (no link to libcuda).
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+
+int current_context_id(unsigned long long* id) {
+  static CtxGetIdFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    int rc = cuda_check(cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q),
+                        "lbm_population_sums_noalloc: driver entry point cuCtxGetId");
+    if (rc) return rc;
+    if (q != cudaDriverEntryPointSuccess || !p)
+      return fail(LBM_ERR_UNSUPPORTED, "lbm_population_sums_noalloc: the driver has no cuCtxGetId");
+    fn = (CtxGetIdFn)p;
+  }
+  // no current context: a plain status, the caller decides whether that is an error
+  return fn(nullptr, id) == 0 ? LBM_OK : LBM_ERR_CUDA;
+}
 
 int noalloc_scratch_address(void** out) {
   int dev = 0;
@@ -878,14 +1058,22 @@ int noalloc_scratch_address(void** out) {
   if (dev < 0 || dev >= kMaxDevices)
     return fail(LBM_ERR_UNSUPPORTED, "lbm_population_sums_noalloc: device %d beyond %d", dev, kMaxDevices);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_address[dev]) {
+  NoAllocSlot& slot = g_noalloc_slot[dev];
+  unsigned long long ctx = 0;
+  // before the runtime has made a context current on this thread the id is
+  // unavailable; the lookup below makes the device's primary context current
+  bool have_ctx = slot.address && current_context_id(&ctx) == LBM_OK;
+  if (!have_ctx || ctx != slot.context_id) {
     void* p = nullptr;
     rc = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_partials),
                     "lbm_population_sums_noalloc: cudaGetSymbolAddress");
     if (rc) return rc;
-    g_noalloc_address[dev] = p;
+    if (current_context_id(&ctx) != LBM_OK)
+      return fail(LBM_ERR_CUDA, "lbm_population_sums_noalloc: no current context after the symbol lookup");
+    slot.context_id = ctx;
+    slot.address = p;
   }
-  *out = g_noalloc_address[dev];
+  *out = slot.address;
   return LBM_OK;
 }
 

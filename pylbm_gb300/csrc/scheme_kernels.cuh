@@ -570,18 +570,31 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_transport(const S* __restrict__ f
   for (int k = 0; k < LBM_Q; ++k) fnew[o + (long long)k * a.g.vstride] = f[o + a.pull[k]];
 }
 
+// Arithmetic of the moment transforms.  Shifted storage holds deviations
+// g = f - feq(c0), whose moments M g are small: they are computed in the
+// module's FP32 arithmetic (the step kernel's own algebra) and the FP64
+// moments of the shift, mref = M feq(c0), are added once per moment, so the
+// float64 moment array costs one conversion and one add per written moment
+// instead of FP64 algebra per node (GB300's FP64 rate is a small fraction of
+// its FP32 rate).  Unshifted storage keeps the whole transform in FP64.
+#if LBM_SHIFTED
+using RM = R;
+#else
+using RM = double;
+#endif
+
 __global__ void __launch_bounds__(LBM_BLOCK) k_f2m(const S* __restrict__ f, double* __restrict__ m,
                                                    MomentArgs a) {
   int i0, i1, i2;
   if (!my_cell(a.g, i0, i1, i2)) return;
   const long long o = lbm::node_offset(a.g, i0, i1, i2);
   const long long om = lbm::node_offset(a.gm, i0, i1, i2);
-  double g[LBM_Q], mm[LBM_Q];
+  RM g[LBM_Q], mm[LBM_Q];
 #pragma unroll
-  for (int k = 0; k < LBM_Q; ++k) g[k] = (double)Store<S>::load(f + o + (long long)k * a.g.vstride);
-  lbm_moments<double>(g, mm);
+  for (int k = 0; k < LBM_Q; ++k) g[k] = (RM)Store<S>::load(f + o + (long long)k * a.g.vstride);
+  lbm_moments<RM>(g, mm);
 #pragma unroll
-  for (int k = 0; k < LBM_Q; ++k) m[om + (long long)k * a.gm.vstride] = mm[k] + lbm_dev_mref[k];
+  for (int k = 0; k < LBM_Q; ++k) m[om + (long long)k * a.gm.vstride] = (double)mm[k] + lbm_dev_mref[k];
 }
 
 // the conserved moments alone (what output and conservation checks read): the
@@ -592,12 +605,12 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_f2m_conserved(const S* __restrict
   if (!my_cell(a.g, i0, i1, i2)) return;
   const long long o = lbm::node_offset(a.g, i0, i1, i2);
   const long long om = lbm::node_offset(a.gm, i0, i1, i2);
-  double g[LBM_Q], mm[LBM_Q];
+  RM g[LBM_Q], mm[LBM_Q];
 #pragma unroll
-  for (int k = 0; k < LBM_Q; ++k) g[k] = (double)Store<S>::load(f + o + (long long)k * a.g.vstride);
-  lbm_moments<double>(g, mm);
+  for (int k = 0; k < LBM_Q; ++k) g[k] = (RM)Store<S>::load(f + o + (long long)k * a.g.vstride);
+  lbm_moments<RM>(g, mm);
 #pragma unroll
-  for (int k = 0; k < LBM_NCONS; ++k) m[om + (long long)k * a.gm.vstride] = mm[k] + lbm_dev_mref[k];
+  for (int k = 0; k < LBM_NCONS; ++k) m[om + (long long)k * a.gm.vstride] = (double)mm[k] + lbm_dev_mref[k];
 }
 
 __global__ void __launch_bounds__(LBM_BLOCK) k_m2f(const double* __restrict__ m, S* __restrict__ f,
@@ -606,13 +619,13 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_m2f(const double* __restrict__ m,
   if (!my_cell(a.g, i0, i1, i2)) return;
   const long long o = lbm::node_offset(a.g, i0, i1, i2);
   const long long om = lbm::node_offset(a.gm, i0, i1, i2);
-  double mm[LBM_Q], g[LBM_Q];
+  RM mm[LBM_Q], g[LBM_Q];
+  // M^-1 (m - mref) = f - shift: the stored deviations directly
 #pragma unroll
-  for (int k = 0; k < LBM_Q; ++k) mm[k] = m[om + (long long)k * a.gm.vstride];
-  lbm_populations<double>(mm, g);
+  for (int k = 0; k < LBM_Q; ++k) mm[k] = (RM)(m[om + (long long)k * a.gm.vstride] - lbm_dev_mref[k]);
+  lbm_populations<RM>(mm, g);
 #pragma unroll
-  for (int k = 0; k < LBM_Q; ++k)
-    Store<S>::store(f + o + (long long)k * a.g.vstride, (R)(g[k] - lbm_dev_shift[k]));
+  for (int k = 0; k < LBM_Q; ++k) Store<S>::store(f + o + (long long)k * a.g.vstride, (R)g[k]);
 }
 
 __global__ void __launch_bounds__(LBM_BLOCK) k_equilibrium(double* __restrict__ m, MomentArgs a) {
@@ -640,7 +653,10 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_relaxation(double* __restrict__ m
 }
 
 // ------------------------------------------------------------------ host
-inline int check_pop_lattice(const lbm_lattice* lat, const char* who) {
+// need_halo: the stencil reach in ghost layers, for the kernels that pull
+// neighbours; the pointwise transforms (f2m, m2f) take any halo, including
+// none (pylbm evaluates its boundary equilibria on such arrays).
+inline int check_pop_lattice(const lbm_lattice* lat, const char* who, bool need_halo = true) {
   int rc = lbm::check_lattice(lat, who);
   if (rc) return rc;
   if (lat->dim != LBM_DIM || lat->nv != LBM_Q)
@@ -648,7 +664,7 @@ inline int check_pop_lattice(const lbm_lattice* lat, const char* who) {
                      lat->nv, LBM_DIM, LBM_Q);
   if (lat->dtype != Store<S>::code)
     return lbm::fail(LBM_ERR_ARG, "%s: lattice dtype %d, module stores %d", who, lat->dtype, Store<S>::code);
-  for (int d = 0; d < LBM_DIM; ++d)
+  for (int d = 0; d < LBM_DIM && need_halo; ++d)
     if (lat->halo[d] < LBM_VMAX)
       return lbm::fail(LBM_ERR_ARG, "%s: halo[%d]=%d below the stencil reach %d", who, d, lat->halo[d], LBM_VMAX);
   return LBM_OK;
@@ -779,7 +795,7 @@ static lbm_scheme::MomentArgs make_moment_args(const lbm_lattice* lat, const lbm
 
 int lbm_f2m(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat, void* stream) {
   using namespace lbm_scheme;
-  int rc = check_pop_lattice(lat, "lbm_f2m");
+  int rc = check_pop_lattice(lat, "lbm_f2m", false);
   if (!rc) rc = check_moment_lattice(lat, mlat, "lbm_f2m");
   if (rc) return rc;
   if (!f || !m) return lbm::fail(LBM_ERR_ARG, "lbm_f2m: NULL buffer");
@@ -790,7 +806,7 @@ int lbm_f2m(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice*
 
 int lbm_f2m_conserved(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat, void* stream) {
   using namespace lbm_scheme;
-  int rc = check_pop_lattice(lat, "lbm_f2m_conserved");
+  int rc = check_pop_lattice(lat, "lbm_f2m_conserved", false);
   if (!rc) rc = check_moment_lattice(lat, mlat, "lbm_f2m_conserved");
   if (rc) return rc;
   if (!f || !m) return lbm::fail(LBM_ERR_ARG, "lbm_f2m_conserved: NULL buffer");
@@ -801,7 +817,7 @@ int lbm_f2m_conserved(const void* f, const lbm_lattice* lat, double* m, const lb
 
 int lbm_m2f(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat, void* stream) {
   using namespace lbm_scheme;
-  int rc = check_pop_lattice(lat, "lbm_m2f");
+  int rc = check_pop_lattice(lat, "lbm_m2f", false);
   if (!rc) rc = check_moment_lattice(lat, mlat, "lbm_m2f");
   if (rc) return rc;
   if (!f || !m) return lbm::fail(LBM_ERR_ARG, "lbm_m2f: NULL buffer");

@@ -100,7 +100,9 @@ class DeviceArray:
     def __init__(self, nv, nspace, vmax, dtype="float64", shift=None):
         self.nv = int(nv)
         self.nspace = [int(n) for n in nspace]
-        self.vmax = [int(v) for v in vmax]
+        # one ghost width per axis, or one for every axis (pylbm passes 0 for
+        # the boundary-value arrays of prepare_rhs, boundary.py:276-281)
+        self.vmax = [int(v) for v in np.broadcast_to(np.atleast_1d(vmax), (len(self.nspace),))]
         self.dim = len(self.nspace)
         self.dtype = dtype
         shape_in = [n - 2 * h for n, h in zip(self.nspace, self.vmax)]
@@ -137,6 +139,40 @@ class DeviceArray:
         self._view(plane)[...] = values - shift.reshape((-1,) + (1,) * self.dim)
         self.buffer.upload(to_storage(plane, self.dtype))
 
+    @property
+    def size(self):
+        return int(np.prod(self.shape))
+
+    def copy(self):
+        """A new device array with the same values (pylbm's Bouzidi methods
+        pass ``fcopy = f.copy()``, boundary.py:549; the kernels keep the copy
+        semantics themselves and do not read it)."""
+        out = DeviceArray(self.nv, self.nspace, self.vmax, self.dtype,
+                          shift=[self.lattice.shift[k] for k in range(self.nv)])
+        out[:] = self
+        return out
+
+    def __getitem__(self, key):
+        """``a[:]`` is the whole array (pylbm copies F into Fnew with
+        ``Fnew.array[:] = F.array[:]``, simulation.py:320)."""
+        if key == slice(None) or key is Ellipsis:
+            return self
+        return self.get()[key]
+
+    def __setitem__(self, key, value):
+        if not (key == slice(None) or key is Ellipsis):
+            host = self.get()
+            host[key] = value
+            self.set(host)
+        elif isinstance(value, DeviceArray):
+            if value.shape != self.shape or value.dtype != self.dtype:
+                raise ValueError("device copy between arrays of different shape or type")
+            runtime.check(runtime.core().lbm_memcpy(self.buffer.handle, value.buffer.handle,
+                                                    self.buffer.nbytes, runtime.D2D, None))
+            runtime.check(runtime.core().lbm_device_synchronize())
+        else:
+            self.set(value)
+
     def free(self):
         self.buffer.free()
 
@@ -172,6 +208,16 @@ class LinkArray:
 
     def get(self):
         return self.host.copy()
+
+    def __getitem__(self, key):
+        """Read the host copy (pylbm's set_rhs reads istore[:, 0] after move2gpu)."""
+        return self.host[key]
+
+    def __setitem__(self, key, value):
+        """Write the host copy and upload it (pylbm's set_rhs assigns rhs[:] every step)."""
+        host = self.host.copy()
+        host[key] = value
+        self.set(host)
 
     def free(self):
         self.buffer.free()

@@ -216,6 +216,10 @@ def core():
             _sig(lib, "lbm_update_halo", I32, [P, LP, P])
             _sig(lib, "lbm_update_halo_axis", I32, [P, LP, I32, P])
             _sig(lib, "lbm_gather", I32, [P, LP, I32, P, P, P, P, P])
+            _sig(lib, "lbm_copy_planes", I32, [P, LP, I32, I32, I32, P, I32, P])
+            _sig(lib, "lbm_fp64_fma_scratch_bytes", I32, [ctypes.POINTER(SZ)])
+            _sig(lib, "lbm_fp64_fma_rate", I32, [P, I32, ctypes.POINTER(ctypes.c_double),
+                                                 ctypes.POINTER(ctypes.c_float), P])
             _sig(lib, "lbm_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_anti_bounce_back", I32, [P, P, P, I32, P, LP, I32, P])
             _sig(lib, "lbm_neumann", I32, [P, P, P, I32, LP, I32, P])
@@ -361,6 +365,38 @@ class PinnedBuffer:
             self.free()
         except Exception:
             pass
+
+
+def fp64_fma_rate(iters=4096, stream=None):
+    """Measured FP64 FMA rate of the current device in flop/s (lbm_fp64_fma_rate)."""
+    lib = core()
+    size = ctypes.c_size_t()
+    check(lib.lbm_fp64_fma_scratch_bytes(ctypes.byref(size)))
+    scratch = DeviceBuffer(size.value)
+    rate, ms = ctypes.c_double(), ctypes.c_float()
+    check(lib.lbm_fp64_fma_rate(scratch.handle, int(iters), ctypes.byref(rate), ctypes.byref(ms), stream))
+    scratch.free()
+    return float(rate.value)
+
+
+class _PinnedArray(np.ndarray):
+    """numpy array over page-locked memory; keeps its PinnedBuffer alive."""
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """Uninitialised numpy array in page-locked host memory.
+
+    Host-device copies from or into such an array run at the link's full
+    rate (pageable memory is staged through driver buffers); pass it to
+    ``Simulation.m_halo[...] = array`` or ``Simulation.fields(out=array)``.
+    """
+    dtype = np.dtype(dtype)
+    shape = tuple(int(n) for n in np.atleast_1d(shape))
+    count = int(np.prod(shape))
+    buf = PinnedBuffer(max(count * dtype.itemsize, 1))
+    arr = buf.array(dtype, count).reshape(shape).view(_PinnedArray)
+    arr._pinned = buf
+    return arr
 
 
 class SchemeModule:

@@ -669,16 +669,52 @@ class Simulation:
         self.module.call(self.module.lib.lbm_relaxation(self._mbuf().handle, ctypes.byref(self._mlat),
                                                         prm.ctypes.data_as(ctypes.c_void_p), self._stream))
 
-    def _set_moment_halo(self, key, value):
+    def _plane_range(self, key):
+        """(first, count, is_slice) of the moment planes a key names: an index,
+        a conserved-moment symbol, or a slice of consecutive planes."""
+        if isinstance(key, slice):
+            r = range(*key.indices(self.scheme.nv))
+            if len(r) == 0 or r.step != 1:
+                raise IndexError("moment planes must be a non-empty run of consecutive indices")
+            return r.start, len(r), True
         idx = self.scheme.consm[key] if isinstance(key, (sp.Symbol, sp.IndexedBase)) else int(key)
-        self._moments_for(None)  # every other plane current before this one changes
-        cur = self._moment_halo(idx)
-        cur[...] = value
-        plane = np.zeros(self._mlat.vstride, dtype=np.float64)
-        self._plane_view(plane, self._mlat)[...] = cur
-        self._mbuf().upload(plane, offset=idx * self._mlat.vstride * 8, stream=self._stream)
-        self._m_cache[idx] = cur
+        if not 0 <= idx < self.scheme.nv:
+            raise IndexError(f"moment {idx} of {self.scheme.nv}")
+        return idx, 1, False
+
+    def _stage(self, nbytes):
+        """Dense device staging buffer of at least ``nbytes`` (kept between calls)."""
+        cur = getattr(self, "_stage_buf", None)
+        if cur is None or cur.nbytes < nbytes:
+            if cur is not None:
+                self.synchronize()
+                cur.free()
+            self._stage_buf = cur = runtime.DeviceBuffer(nbytes)
+        return cur
+
+    def _set_moment_halo(self, key, value):
+        """The named plane(s) of the moment array take ``value`` (broadcast to
+        the halo box); the other planes stay as they are (pylbm/simulation.py:
+        210-213).  The dense array crosses to the device in one copy (at the
+        link's full rate from pinned memory, ``runtime.pinned_empty``) and a
+        kernel writes it into the padded layout."""
+        if self._need_init:
+            self._initialize()
+        first, count, many = self._plane_range(key)
+        shape = ((count,) if many else ()) + tuple(self.domain.shape_halo)
+        src = np.asarray(value)
+        if src.dtype != np.float64 or src.shape != shape or not src.flags["C_CONTIGUOUS"]:
+            src = np.ascontiguousarray(np.broadcast_to(src.astype(np.float64, copy=False), shape))
+        stage = self._stage(src.nbytes)
+        runtime.check(self._core.lbm_memcpy(stage.handle, src.ctypes.data_as(ctypes.c_void_p), src.nbytes,
+                                            runtime.H2D, self._stream))
+        runtime.check(self._core.lbm_copy_planes(self._mbuf().handle, ctypes.byref(self._mlat), first, count, 1,
+                                                 stage.handle, 1, self._stream))
+        self.synchronize()  # ``value`` may be a temporary
+        for i in range(first, first + count):
+            self._m_cache.pop(i, None)
         self._update_m = False
+        self._m_partial = False
 
     def _drop_graph(self):
         if self._graph is not None:
@@ -754,9 +790,32 @@ class Simulation:
                     self._m_cache[first + j] = np.array(self._plane_view(plane, self._mlat))
         return self._m_cache[idx]
 
-    def fields(self):
-        """Conserved moments on the interior, {name: array}, read with one device-to-host copy."""
-        return {str(c): self.m[c] for c in self.scheme.consm}
+    def fields(self, out=None):
+        """Conserved moments on the interior, {name: array}.
+
+        One launch computes the conserved moments, one gathers their interior
+        nodes into a dense device array, and one device-to-host copy brings
+        them over: into ``out`` when given (float64, shape (nconsm, *interior),
+        C-contiguous; page-locked memory from ``runtime.pinned_empty`` copies
+        at the link's full rate), else into a new array.
+        """
+        if self._need_init:
+            self._initialize()
+        nc = self.scheme.nconsm
+        shape = (nc,) + tuple(self.domain.shape_in)
+        if out is None:
+            out = np.empty(shape, dtype=np.float64)
+        elif out.shape != shape or out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"fields(out=...) needs a C-contiguous float64 array of shape {shape}")
+        self._moments_for(0)
+        stage = self._stage(out.nbytes)
+        runtime.check(self._core.lbm_copy_planes(self._mbuf().handle, ctypes.byref(self._mlat), 0, nc, 0,
+                                                 stage.handle, 0, self._stream))
+        runtime.check(self._core.lbm_memcpy(out.ctypes.data_as(ctypes.c_void_p), stage.handle, out.nbytes,
+                                            runtime.D2H, self._stream))
+        self.synchronize()
+        names = sorted(self.scheme.consm.items(), key=lambda kv: kv[1])
+        return {str(c): out[i] for c, i in names}
 
     def write_h5(self, filename, path="", timestep=None, vectors=None):
         """Write the conserved moments (and {name: [moment names]} vectors) as
@@ -891,7 +950,7 @@ class Simulation:
 
     def free(self):
         self._drop_graph()
-        for b in (self._F, self._Fnew, self._M):
+        for b in (self._F, self._Fnew, self._M, getattr(self, "_stage_buf", None)):
             if b is not None:
                 b.free()
         self._free_bc()

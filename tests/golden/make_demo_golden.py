@@ -4,7 +4,7 @@ Run in a container where the reference sources are available (read-only) and
 Cython is installed:
 
     PYTHONDONTWRITEBYTECODE=1 \
-    PYTHONPATH=oracle/shims:/root/reference python tests/golden/make_demo_golden.py [case ...]
+    PYTHONPATH=oracle/shims:$PYLBM_REFERENCE python tests/golden/make_demo_golden.py [case ...]
 
 For every case of tests/demo_cases.py this script
 1. reads the reference's HDF5 golden file with h5lite (fields stored
@@ -30,7 +30,7 @@ import sympy as sp
 HERE = os.path.dirname(os.path.abspath(__file__))
 TESTS = os.path.dirname(HERE)
 ROOT = os.path.dirname(TESTS)
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("PYLBM_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
 sys.path.insert(0, ROOT)
 sys.path.insert(0, TESTS)
 sys.path.insert(0, HERE)

@@ -4,7 +4,7 @@ Run in a container where the reference sources are available (read-only) and
 Cython is installed:
 
     PYTHONDONTWRITEBYTECODE=1 \
-    PYTHONPATH=oracle/shims:/root/reference python tests/golden/make_golden.py
+    PYTHONPATH=oracle/shims:$PYLBM_REFERENCE python tests/golden/make_golden.py
 
 The shims in oracle/shims stand in for mpi4py (one rank), cerberus,
 colorlog, colorama, h5py, matplotlib and numpy-stl, which pylbm imports but

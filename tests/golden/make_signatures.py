@@ -10,7 +10,7 @@ with ``pylbm_gb300.generator.CudaModule``.  Run where the reference sources
 and Cython are available:
 
     PYTHONDONTWRITEBYTECODE=1 \\
-    PYTHONPATH=oracle/shims:/root/reference python tests/golden/make_signatures.py
+    PYTHONPATH=oracle/shims:$PYLBM_REFERENCE python tests/golden/make_signatures.py
 """
 import inspect
 import json

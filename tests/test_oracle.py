@@ -91,15 +91,11 @@ def test_reference_kernel_baseline_computes_the_step():
     if mod is None:
         pytest.skip("oracle/_ref not generated (needs the reference sources and Cython)")
     n = 12
-    f = ref_baseline._slab_state(n, 0, n)
-    fnew = np.empty_like(f)
-    for _ in range(3):
-        ref_baseline._halo(f)
-        mod.one_time_step(f, fnew, *f.shape[:3])
-        f, fnew = fnew, f
+    # one slab process: one untimed step and two timed ones
+    _, _, f = ref_baseline.run_slabs(n=n, steps=2, procs=1, keep_state=True)
     o = OracleSimulation(W.tgv3d(n=n))
     o.run(3)
-    got = np.moveaxis(f, -1, 0)[:, 1:-1, 1:-1, 1:-1]
+    got = np.moveaxis(f, -1, 0)
     assert np.abs(got - o.f[:, 1:-1, 1:-1, 1:-1]).max() < 1e-13
 
 
