@@ -409,11 +409,15 @@ int lbm_one_time_step_periodic(const void* f, void* fnew, const lbm_lattice* lat
  * receive corr_j = y_j * sig_out[j] + mu_out[j], y = MLP((m - mu_in) * isig_in)
  * of the node's pre-collision moments m.  norm (host, 48 floats): mu_in[16],
  * isig_in[16], mu_out[8], sig_out[8].  wbf16/params: the MLP blocks of
- * lbm_mlp_* (device).  grid > 0 caps the number of blocks (persistent
- * loop).  Needs nv <= 16 and nv - nconsm <= 8. */
+ * lbm_mlp_* (device).  guard (host, 2 floats, or NULL for none): a node
+ * whose corrections are not all finite and within guard[0] * (the largest
+ * change the relaxation made to its non-conserved moments) + guard[1] keeps
+ * the plain MRT collision (bit for bit that of lbm_one_time_step_periodic)
+ * and adds one to *fallbacks (device int32, or NULL).  grid > 0 caps the
+ * number of blocks (persistent loop).  Needs nv <= 16 and nv - nconsm <= 8. */
 int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
-                                       const void* wbf16, const float* params, const float* norm, int32_t grid,
-                                       void* stream);
+                                       const void* wbf16, const float* params, const float* norm,
+                                       const float* guard, int32_t* fallbacks, int32_t grid, void* stream);
 
 /* Pure pull streaming on the interior (pylbm/algorithm/base.py:289-296). */
 int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* stream);
@@ -438,6 +442,13 @@ int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void*
 
 /* Moment-space relaxation m <- m + s (m_eq - m) (pylbm/algorithm/base.py:404-437). */
 int lbm_relaxation(double* m, const lbm_lattice* mlat, const double* prm, void* stream);
+
+/* Source terms over half a time step on the interior nodes: each conserved
+ * moment with a source gets m_c += dt/2 S_c(m) (explicit Euler,
+ * pylbm/algorithm/base.py:439-504 and algorithm/ode.py:11-16; dt is the
+ * run-time parameter "dt").  LBM_ERR_UNSUPPORTED for schemes without
+ * source terms (pylbm generates no source_term routine for them). */
+int lbm_source_term(double* m, const lbm_lattice* mlat, const double* prm, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* Batched ensembles: many independent periodic simulations of one    */

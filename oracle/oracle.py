@@ -302,6 +302,21 @@ class OracleSimulation:
         inner = tuple(slice(int(h[d]), int(h[d]) + int(n[d])) for d in range(dim))
         self.fnew[(slice(None),) + inner] = np.tensordot(self.invM, m, axes=1)
 
+    def source_term(self, m):
+        """pylbm's standalone source_term (pylbm/algorithm/base.py:439-504,
+        ode.py:11-16) on a halo-box moment array m[nv, ...]: every conserved
+        moment with a source gets m_c + dt/2 S_c(m) on the interior nodes, from
+        the moments as they were; returns a new array."""
+        fn = self._frame_functions()
+        out = np.array(m, dtype=np.float64)
+        inner = tuple(slice(int(self.h[d]), int(self.h[d]) + int(self.n[d])) for d in range(self.dim))
+        mi = [out[(k,) + inner] for k in range(self.scheme.nv)]
+        zero = np.zeros_like(mi[0])
+        new = [(k, zero + f(*mi, *([zero] * self.dim))) for k, f in fn["src"]]
+        for k, v in new:
+            out[(k,) + inner] = v
+        return out
+
     def moments_halo(self):
         sc = self.scheme
         m = np.zeros_like(self.f)

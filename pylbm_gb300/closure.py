@@ -163,9 +163,16 @@ class ClosureModel:
         self.meta = dict(meta or {})
         sm, _ = runtime.device_info()
         self.grid = 2 * sm  # fused closure step: persistent blocks, two per SM
+        # guard of the fused step: corrections beyond 8x the relaxation's own
+        # change plus 8 output standard deviations (or not finite) fall back
+        # to the plain collision at that node
+        self.guard = np.array([8.0, 8.0 * float(np.max(self.norm[40:48]))], dtype=np.float32)
 
     def norm_ptr(self):
         return self.norm.ctypes.data_as(ctypes.c_void_p)
+
+    def guard_ptr(self):
+        return self.guard.ctypes.data_as(ctypes.c_void_p)
 
     def save(self, path):
         np.savez(path, params=self.mlp.params_host(), norm=self.norm,

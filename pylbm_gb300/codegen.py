@@ -601,6 +601,7 @@ class SchemeSource:
         out += self._relax_abs_code("m")
         out.append("  (void)prm;")
         out.append("}")
+        out += self._source_half_function()
         out.append("template <typename R>")
         out.append("__device__ __forceinline__ void lbm_collide(R (&g)[LBM_Q], const R* __restrict__ prm) {")
         if self.absolute_collide:
@@ -637,7 +638,19 @@ class SchemeSource:
         out += fn("lbm_equilibrium_abs(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.equilibrium("m"))
         out += fn("lbm_collide(R (&g)[LBM_Q], const R* __restrict__ prm)",
                   ["R m[LBM_Q];"] + ref.moments_pull("g", "m") + ref.relaxation("m") + ref.populations("m", "g"))
+        out += self._source_half_function()
         return out
+
+    def _source_half_function(self):
+        """pylbm's standalone source_term on absolute moments: m_c += dt/2 S_c(m)
+        (pylbm/algorithm/base.py:439-504 with ode.py:11-16); empty without
+        source terms."""
+        body = self._source_code(self._names(), "  ")
+        return ["// source terms over half a time step (absolute moments)",
+                f"#define LBM_HAS_SOURCE {1 if self.scheme.source_terms else 0}",
+                "template <typename R>",
+                "__device__ __forceinline__ void lbm_source_half(R (&m)[LBM_Q], const R* __restrict__ prm) {"] + \
+            body + ["  (void)m;", "  (void)prm;", "}"]
 
     def module_source(self, storage, compute):
         """Full translation unit of the module for one storage/compute type (memoised:

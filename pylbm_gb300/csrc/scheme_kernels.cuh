@@ -454,6 +454,11 @@ struct ClosureArgs {
   float mu_in[16], isig_in[16];
   float mu_out[8], sig_out[8];
   long long nodes;         // interior nodes
+  // guard: a node whose corrections are not finite or exceed
+  // ratio * (largest change the relaxation itself made) + floor keeps the
+  // plain MRT collision and is counted (ratio <= 0: no guard)
+  float guard_ratio, guard_floor;
+  int* fallbacks;          // device counter of guarded nodes, or null
 };
 
 constexpr int kClosureWarps = 8;
@@ -548,10 +553,29 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
     }
     __syncwarp();
     if (active) {
-      lbm_relax<R>(m, a.prm);
+      R pre[LBM_Q - LBM_NCONS];
 #pragma unroll
-      for (int j = 0; j < LBM_Q - LBM_NCONS; ++j)
-        m[LBM_NCONS + j] += (R)(y_s[warp][lane * OUT + j] * c.sig_out[j] + c.mu_out[j]);
+      for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) pre[j] = m[LBM_NCONS + j];
+      lbm_relax<R>(m, a.prm);
+      float corr[LBM_Q - LBM_NCONS];
+      float change = 0.0f;
+#pragma unroll
+      for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) {
+        corr[j] = y_s[warp][lane * OUT + j] * c.sig_out[j] + c.mu_out[j];
+        change = fmaxf(change, fabsf((float)(m[LBM_NCONS + j] - pre[j])));
+      }
+      bool ok = true;
+      if (c.guard_ratio > 0.0f) {
+        const float limit = c.guard_ratio * change + c.guard_floor;
+#pragma unroll
+        for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) ok = ok && fabsf(corr[j]) <= limit;  // false for NaN
+      }
+      if (ok) {
+#pragma unroll
+        for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) m[LBM_NCONS + j] += (R)corr[j];
+      } else if (c.fallbacks) {
+        atomicAdd(c.fallbacks, 1);
+      }
       lbm_populations<R>(m, gv);
 #pragma unroll
       for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * g.vstride, gv[k]);
@@ -650,6 +674,20 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_relaxation(double* __restrict__ m
   lbm_relax_abs<double>(mm, a.prm);
 #pragma unroll
   for (int k = LBM_NCONS; k < LBM_Q; ++k) m[om + (long long)k * a.gm.vstride] = mm[k];
+}
+
+// pylbm's standalone source_term: the conserved moments of the interior
+// nodes advance over half a time step by explicit Euler
+__global__ void __launch_bounds__(LBM_BLOCK) k_source_term(double* __restrict__ m, MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_node(a.gm, i0, i1, i2)) return;
+  const long long om = lbm::node_offset(a.gm, i0, i1, i2);
+  double mm[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) mm[k] = m[om + (long long)k * a.gm.vstride];
+  lbm_source_half<double>(mm, a.prm);
+#pragma unroll
+  for (int k = 0; k < LBM_NCONS; ++k) m[om + (long long)k * a.gm.vstride] = mm[k];
 }
 
 // ------------------------------------------------------------------ host
@@ -837,9 +875,21 @@ int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void*
   return lbm::launch_check("lbm_equilibrium");
 }
 
+int lbm_source_term(double* m, const lbm_lattice* mlat, const double* prm, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_moment_lattice(nullptr, mlat, "lbm_source_term");
+  if (rc) return rc;
+  if (!LBM_HAS_SOURCE) return lbm::fail(LBM_ERR_UNSUPPORTED, "lbm_source_term: the scheme has no source terms");
+  if (!m) return lbm::fail(LBM_ERR_ARG, "lbm_source_term: NULL buffer");
+  if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "lbm_source_term: parameters expected");
+  MomentArgs a = make_moment_args(nullptr, mlat, prm);
+  k_source_term<<<node_grid(*mlat, false), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, a);
+  return lbm::launch_check("lbm_source_term");
+}
+
 int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
-                                       const void* wbf16, const float* params, const float* norm, int32_t grid,
-                                       void* stream) {
+                                       const void* wbf16, const float* params, const float* norm,
+                                       const float* guard, int32_t* fallbacks, int32_t grid, void* stream) {
   using namespace lbm_scheme;
   const char* who = "lbm_one_time_step_periodic_closure";
   int rc = check_pop_lattice(lat, who);
@@ -861,6 +911,9 @@ int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_latt
     c.sig_out[i] = norm[40 + i];
   }
   c.nodes = (long long)lat->n[0] * lat->n[1] * lat->n[2];
+  c.guard_ratio = guard ? guard[0] : 0.0f;
+  c.guard_floor = guard ? guard[1] : 0.0f;
+  c.fallbacks = fallbacks;
   const long long per = 16 * kClosureWarps;
   long long blocks = (c.nodes + per - 1) / per;
   if (grid > 0 && blocks > grid) blocks = grid;

@@ -16,6 +16,7 @@ routine                    reference (pylbm/...)                        C ABI
 one_time_step              algorithm/base.py:551-600, pull.py:11-59     lbm_one_time_step
 f2m / m2f                  algorithm/base.py:336-360                    lbm_f2m / lbm_m2f
 equilibrium / relaxation   algorithm/base.py:298-335,361-402            lbm_equilibrium / lbm_relaxation
+source_term                algorithm/base.py:439-504                    lbm_source_term
 transport                  algorithm/base.py:403-428                    lbm_transport
 bounce_back                boundary.py:400-469                          lbm_bounce_back
 anti_bounce_back           boundary.py:626-684                          lbm_anti_bounce_back
@@ -82,6 +83,10 @@ def routine_signatures(scheme):
         "Bouzidi_bounce_back": ["dist", "f", "fcopy", "iload0", "iload1", "istore", "ncond"] + space + ["rhs"],
         "Bouzidi_anti_bounce_back": ["dist", "f", "iload0", "iload1", "istore", "ncond"] + space + ["rhs"],
     }
+    if scheme.source_terms:
+        # pylbm generates source_term only for schemes with sources (base.py:616-617)
+        src = {"dt"} | {str(s) for _, e in scheme.source_terms for s in getattr(e, "free_symbols", ())}
+        sig["source_term"] = ["m"] + space + prm(src)
     for a in space:
         sig["neumann" + a[1]] = list(links)
         sig["update_" + a[1]] = ["f"] + space + ["nv"]
@@ -259,6 +264,7 @@ class CudaModule:
         impl = {
             "one_time_step": self._one_time_step, "f2m": self._f2m, "m2f": self._m2f,
             "equilibrium": self._equilibrium, "relaxation": self._relaxation, "transport": self._transport,
+            "source_term": self._source_term,
             "bounce_back": self._bounce_back, "anti_bounce_back": self._anti_bounce_back,
             "Bouzidi_bounce_back": self._bouzidi_bounce_back,
             "Bouzidi_anti_bounce_back": self._bouzidi_anti_bounce_back,
@@ -357,6 +363,12 @@ class CudaModule:
         prm = self._prm(kw)
         self.module.call(self.module.lib.lbm_relaxation(m.ptr, self._check(m, kw, "m"),
                                                         prm.ctypes.data_as(ctypes.c_void_p), None))
+
+    def _source_term(self, **kw):
+        m = kw["m"]
+        prm = self._prm(kw)
+        self.module.call(self.module.lib.lbm_source_term(m.ptr, self._check(m, kw, "m"),
+                                                         prm.ctypes.data_as(ctypes.c_void_p), None))
 
     def _transport(self, **kw):
         f, fnew = kw["f"], kw["fnew"]

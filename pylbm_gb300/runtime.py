@@ -453,9 +453,10 @@ class SchemeModule:
         _sig(lib, "lbm_m2f", I32, [P, LP, P, LP, P])
         _sig(lib, "lbm_equilibrium", I32, [P, LP, P, P])
         _sig(lib, "lbm_relaxation", I32, [P, LP, P, P])
+        _sig(lib, "lbm_source_term", I32, [P, LP, P, P])
         _sig(lib, "lbm_ensemble_step", I32, [P, P, P, I32, I32, I32, I32, I32, P])
         _sig(lib, "lbm_ensemble_step_pairs", I32, [P, P, P, I32, I32, I32, I32, I32, P])
-        _sig(lib, "lbm_one_time_step_periodic_closure", I32, [P, P, LP, P, P, P, P, I32, P])
+        _sig(lib, "lbm_one_time_step_periodic_closure", I32, [P, P, LP, P, P, P, P, P, P, I32, P])
 
     def call(self, rc):
         check(rc, self.lib, "lbm_scheme_last_error")

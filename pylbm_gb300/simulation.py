@@ -553,15 +553,28 @@ class Simulation:
         if model is not None and (self.scheme.Tu is not None or self.scheme.source_terms):
             raise ValueError("the learned closure corrects the plain MRT relaxation only")
         self.closure = model
+        if model is not None and getattr(self, "_fallbacks", None) is None:
+            self._fallbacks = runtime.DeviceBuffer(4)
+        if model is not None:
+            self._fallbacks.zero(self._stream)
         self._drop_graph()
+
+    def closure_fallbacks(self):
+        """Node updates since set_closure() at which the closure's guard kept the
+        plain MRT collision (corrections not finite, or far beyond the
+        relaxation's own change)."""
+        if getattr(self, "_fallbacks", None) is None:
+            return 0
+        out = np.zeros(1, dtype=np.int32)
+        self._fallbacks.download(out, stream=self._stream)
+        return int(out[0])
 
     def _launch_step(self, F, Fnew, pp):
         model = getattr(self, "closure", None)
         if model is not None:
-            norm = model.norm_ptr()
             self.module.call(self.module.lib.lbm_one_time_step_periodic_closure(
-                F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.w.handle, model.mlp.p.handle, norm,
-                model.grid, self._stream))
+                F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.w.handle, model.mlp.p.handle,
+                model.norm_ptr(), model.guard_ptr(), self._fallbacks.handle, model.grid, self._stream))
             return
         fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
         self.module.call(fn(F.handle, Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
@@ -668,6 +681,19 @@ class Simulation:
         prm = self._prm()
         self.module.call(self.module.lib.lbm_relaxation(self._mbuf().handle, ctypes.byref(self._mlat),
                                                         prm.ctypes.data_as(ctypes.c_void_p), self._stream))
+
+    def source_term(self, fraction_of_time_step=1.0):
+        """Source terms over half a time step on the moments of the interior
+        (pylbm/simulation.py:336-341: the generated routine integrates
+        m_c += dt/2 S_c(m), pylbm/algorithm/ode.py:11-16, and
+        ``fraction_of_time_step`` is accepted and not used, as there)."""
+        if not self.scheme.source_terms:
+            raise ValueError("the scheme has no source terms")
+        self._moments_ready()
+        self._moments_for(None)
+        prm = self._prm()
+        self.module.call(self.module.lib.lbm_source_term(self._mbuf().handle, ctypes.byref(self._mlat),
+                                                         prm.ctypes.data_as(ctypes.c_void_p), self._stream))
 
     def _plane_range(self, key):
         """(first, count, is_slice) of the moment planes a key names: an index,
@@ -950,7 +976,7 @@ class Simulation:
 
     def free(self):
         self._drop_graph()
-        for b in (self._F, self._Fnew, self._M, getattr(self, "_stage_buf", None)):
+        for b in (self._F, self._Fnew, self._M, getattr(self, "_stage_buf", None), getattr(self, "_fallbacks", None)):
             if b is not None:
                 b.free()
         self._free_bc()

@@ -77,3 +77,21 @@ def test_closure_conserves_mass_and_momentum():
     c1 = sim.conserved_sums()
     assert abs(c1[0] - c0[0]) < 1e-6 * abs(c0[0])
     assert np.all(np.abs(c1[1:] - c0[1:]) < 1e-6 * abs(c0[0]))
+
+
+@pytest.mark.parametrize("bad", ["nan", "huge"])
+def test_guard_keeps_the_plain_collision_for_a_broken_network(bad):
+    """A network whose outputs are not finite (NaN weights) or absurdly large
+    (weights scaled by 1e6) trips the fused step's guard at every node: each
+    node keeps the plain MRT collision, so the run equals the plain run bit
+    for bit, and the fallbacks are counted."""
+    d = W.shear_layer(n=64, nu=1e-3, seed=5)
+    a = Simulation(d, dtype="float32")
+    b = Simulation(d, dtype="float32")
+    p = init_params(11).astype(np.float32)
+    p = np.full_like(p, np.nan) if bad == "nan" else p * 1e6
+    b.set_closure(ClosureModel(p, _norm(scale_out=1e-3)))
+    a.run(12)
+    b.run(12)
+    assert np.array_equal(_moments(a), _moments(b))
+    assert b.closure_fallbacks() == 12 * 64 * 64

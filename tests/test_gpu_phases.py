@@ -71,3 +71,24 @@ def test_phases_compose_to_a_step(case):
     assert np.abs(fa - fb).max() <= 1e-14 * np.abs(fa).max()
     a.free()
     b.free()
+
+
+def test_source_term_against_oracle_half_step():
+    """pylbm's standalone source_term (logistic reaction mu u (1 - u) of the
+    advection-reaction demo): m_c + dt/2 S_c(m) on the interior, ghosts and
+    other moments untouched, against the oracle's restatement."""
+    import demo_cases
+    from oracle import OracleSimulation
+
+    d = demo_cases.advection_reaction_1d(dx=1.0 / 128)
+    sim = Simulation(d)
+    rng = np.random.default_rng(7)
+    m = np.stack([0.5 + 0.3 * rng.standard_normal(sim.domain.shape_halo) for _ in range(sim.scheme.nv)])
+    for k in range(sim.scheme.nv):
+        sim.m_halo[k] = m[k]
+    sim.source_term()
+    got = planes(sim)
+    want = OracleSimulation(d).source_term(m)
+    assert not np.array_equal(want, m)
+    assert np.abs(got - want).max() <= 1e-15 * np.abs(want).max()
+    sim.free()
