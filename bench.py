@@ -158,20 +158,22 @@ def variants(args):
     peak, _ = measured_peaks()
     out = {}
     cases = [
-        ("tgv3d_256_f64", lambda: Simulation(W.tgv3d(n=256), dtype="float64", parity=False), 256 ** 3, 19, 8, 40),
-        ("tgv3d_256_f16", lambda: Simulation(W.tgv3d(n=256), dtype="float16"), 256 ** 3, 19, 2, 100),
-        ("tgv3d_256_bf16", lambda: Simulation(W.tgv3d(n=256), dtype="bfloat16"), 256 ** 3, 19, 2, 100),
-        ("cavity_256_f64_parity", lambda: Simulation(W.cavity(n=256)), 256 ** 2, 9, 8, 1000),
-        ("cylinder_2048x512_f32", lambda: Simulation(W.cylinder(), dtype="float32"), 2048 * 512, 9, 4, 1000),
+        ("tgv3d_256_f64", lambda: W.tgv3d(n=256), "float64", 256 ** 3, 19, 40),
+        ("tgv3d_256_f16", lambda: W.tgv3d(n=256), "float16", 256 ** 3, 19, 100),
+        ("tgv3d_256_bf16", lambda: W.tgv3d(n=256), "bfloat16", 256 ** 3, 19, 100),
+        ("cavity_256_f64_parity", lambda: W.cavity(n=256), "float64", 256 ** 2, 9, 1000),
+        ("cylinder_2048x512_f32", lambda: W.cylinder(), "float32", 2048 * 512, 9, 1000),
         # relative-velocity (Geier) collide, Bouzidi walls and disc, NeumannX outflow
-        ("karman_geier_2048x1024_f32", lambda: Simulation(W.karman(dx=1.0 / 1024), dtype="float32"),
-         2048 * 1024, 9, 4, 500),
+        ("karman_geier_2048x1024_f32", lambda: W.karman(dx=1.0 / 1024), "float32", 2048 * 1024, 9, 500),
         # bounded 3D: bounce-back on all six walls (1.96 M links per step), moving lid
-        ("cavity3d_256_f32", lambda: Simulation(W.cavity3d(n=256), dtype="float32"), 256 ** 3, 19, 4, 100),
-        ("cavity3d_256_f16", lambda: Simulation(W.cavity3d(n=256), dtype="float16"), 256 ** 3, 19, 2, 100),
+        ("cavity3d_256_f32", lambda: W.cavity3d(n=256), "float32", 256 ** 3, 19, 100),
+        ("cavity3d_256_f16", lambda: W.cavity3d(n=256), "float16", 256 ** 3, 19, 100),
     ]
-    for name, make, nodes, q, es, steps in cases:
-        sim = make()
+    for name, dico, dtype, nodes, q, steps in cases:
+        # the FP64 TGV runs the exact-constant form (the faster FP64 path);
+        # the cavity runs the reference generator's printed forms
+        sim = Simulation(dico(), dtype=dtype, parity=name != "tgv3d_256_f64")
+        es = BYTES_PER_VALUE[dtype]
         for _ in range(3):
             sim.one_time_step()
         ms = time_steps(sim, steps)
@@ -179,10 +181,52 @@ def variants(args):
         gbs = 2 * q * es * nodes * steps / (ms / 1e3) / 1e9
         out[name] = {"MLUPS": mlups, "ms_per_step": ms / steps, "GB/s": gbs, "hbm_frac": gbs / peak,
                      "steps": steps}
+        if dtype != "float64":
+            out[name]["err_vs_fp64"] = precision_error(sim, dico)
         sim.free()
     out["tgv3d_256_500_steps_precision"] = tgv_precision()
     out["ensemble_512_d2q9_f16"] = ensemble_variant(peak)
     out["learned_closure_d2q9"] = closure_variant()
+    return out
+
+
+def _velocity_errors(cons, ref, fluid, dim):
+    """Relative L2 errors of velocity (and, in 2D, vorticity) and the largest
+    relative density error over the fluid nodes."""
+    u = np.stack([c / cons[0] for c in cons[1:]])
+    ur = np.stack([c / ref[0] for c in ref[1:]])
+    u = np.where(fluid, u, 0.0)
+    ur = np.where(fluid, ur, 0.0)
+    out = {"velocity_rel_l2": float(np.linalg.norm(u - ur) / np.linalg.norm(ur)),
+           "density_max_rel": float(np.abs(np.where(fluid, cons[0] - ref[0], 0.0)).max() / np.abs(ref[0]).max())}
+    if dim == 2:
+        w = np.gradient(u[1], axis=0) - np.gradient(u[0], axis=1)
+        wr = np.gradient(ur[1], axis=0) - np.gradient(ur[0], axis=1)
+        out["vorticity_rel_l2"] = float(np.linalg.norm(w - wr) / np.linalg.norm(wr))
+    return out
+
+
+def precision_error(sim, dico):
+    """Error of a shifted-storage run against the FP64 run of the same
+    dictionary over the same number of steps (FP64: the reference generator's
+    printed forms where the scheme allows, which reproduce pylbm's Cython)."""
+    from pylbm_gb300 import Simulation
+
+    steps = sim.nt
+    f = sim.fields()
+    cons = np.stack([np.array(v) for v in f.values()])
+    dom = sim.domain
+    fluid = (dom.in_or_out[tuple(slice(int(h), -int(h)) for h in dom.halo)] == dom.valin
+             if dom.in_or_out is not None else np.ones(dom.shape_in, dtype=bool))
+    ref_sim = Simulation(dico(), dtype="float64")
+    ref_sim.run(steps)
+    ref = np.stack([np.array(v) for v in ref_sim.fields().values()])
+    style = ref_sim.module.src.style
+    ref_sim.free()
+    out = {"against": "float64 run of the same dictionary" + (" (pylbm's printed forms)" if style == "reference"
+                                                               else " (exact constants)"),
+           "steps": steps}
+    out.update(_velocity_errors(cons, ref, fluid, sim.dim))
     return out
 
 
@@ -231,6 +275,16 @@ def ensemble_variant(peak, steps=200):
            "GB/s": 36 * nodes * steps / (ms / 1e3) / 1e9, "hbm_frac": 36 * nodes * steps / (ms / 1e3) / 1e9 / peak,
            "instances": len(sides), "nodes_per_step": nodes, "tile": list(ens.tile), "setup_s": setup,
            "steps": steps}
+    # every instance against its own FP64 run of the same length
+    ens64, _, _ = shear_ensemble(count=512, seed=0, dtype="float64", tile=(64, 4, 0))
+    ens64.run(ens.nt)
+    errs = []
+    for i in range(len(sides)):
+        got, ref = ens.moments(i, keys=range(3)), ens64.moments(i, keys=range(3))
+        errs.append(_velocity_errors(got, ref, np.ones(got.shape[1:], dtype=bool), 2)["velocity_rel_l2"])
+    ens64.free()
+    res["err_vs_fp64"] = {"against": "each instance's own float64 run", "steps": ens.nt,
+                          "velocity_rel_l2_max": float(np.max(errs)), "velocity_rel_l2_median": float(np.median(errs))}
     ens.free()
     return res
 
