@@ -183,11 +183,33 @@ def variants(args):
                      "steps": steps}
         if dtype != "float64":
             out[name]["err_vs_fp64"] = precision_error(sim, dico)
+        elif name in FP64_INST_PER_NODE:
+            out[name]["fp64"] = fp64_roof(FP64_INST_PER_NODE[name], nodes * steps / (ms / 1e3))
         sim.free()
     out["tgv3d_256_500_steps_precision"] = tgv_precision()
     out["ensemble_512_d2q9_f16"] = ensemble_variant(peak)
     out["learned_closure_d2q9"] = closure_variant()
     return out
+
+
+# FP64-pipe instructions (DADD + DMUL + DFMA) per node of the FP64 step
+# kernels, from an ncu capture of the same kernels (a property of the compiled
+# code; profiles/ncu_fp64_step_counts.md): the exact-constant D3Q19 form uses
+# 131 DADD + 14 DMUL + 84 DFMA, the printed (parity) D2Q9 form, compiled
+# without contraction, 114 DADD + 33 DMUL
+FP64_INST_PER_NODE = {"tgv3d_256_f64": 229, "cavity_256_f64_parity": 147}
+
+
+def fp64_roof(inst_per_node, nodes_per_s):
+    """The FP64 step against the FP64 pipe: its instruction rate over the
+    measured DFMA instruction rate of this GPU (lbm_fp64_fma_rate)."""
+    from pylbm_gb300 import runtime
+
+    peak_flops = runtime.fp64_fma_rate()
+    achieved = inst_per_node * nodes_per_s
+    return {"inst_per_node": inst_per_node, "inst_source": "ncu capture (profiles/ncu_fp64_step_counts.md)",
+            "achieved_inst_per_s": achieved, "measured_dfma_tflops": peak_flops / 1e12,
+            "pipe_frac": achieved / (peak_flops / 2)}
 
 
 def _velocity_errors(cons, ref, fluid, dim):
@@ -320,8 +342,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256, help="grid size per axis")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "karman", "cavity3d"],
-                    help="tgv: the headline D3Q19 workload; cylinder / karman / cavity3d: the bounded flows")
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "karman", "cavity3d", "cavity"],
+                    help="tgv: the headline D3Q19 workload; cylinder / karman / cavity3d / cavity (D2Q9 n^2): "
+                         "the bounded flows")
+    ap.add_argument("--step-variant", type=int, default=0, choices=[0, 1],
+                    help="16-bit periodic steps: 1 staged kernel where rows fit, 0 direct-load kernel")
+    ap.add_argument("--fp64-form", default="parity", choices=["parity", "exact"],
+                    help="float64 only: the reference generator's printed forms (parity) or exact constants")
     ap.add_argument("--dtype", default="float32", choices=list(BYTES_PER_VALUE))
     ap.add_argument("--cpu-grid", type=int, default=256)
     ap.add_argument("--cpu-steps", type=int, default=10)
@@ -351,8 +378,9 @@ def main():
 
     runtime.check(runtime.core().lbm_set_device(local))
     n = args.n
+    parity = args.fp64_form == "parity"
     if args.workload == "tgv":
-        sim = Simulation(W.tgv3d(n=n), dtype=args.dtype)
+        sim = Simulation(W.tgv3d(n=n), dtype=args.dtype, parity=parity)
         assert sim.periodic
         desc = f"D3Q19 MRT periodic Taylor-Green vortex {n}^3"
     elif args.workload == "cylinder":
@@ -361,9 +389,13 @@ def main():
     elif args.workload == "karman":
         sim = Simulation(W.karman(dx=1.0 / 1024), dtype=args.dtype)
         desc = "D2Q9 Geier relative-velocity flow past a disc 2048x1024 (Bouzidi walls and disc, NeumannX)"
+    elif args.workload == "cavity":
+        sim = Simulation(W.cavity(n=n), dtype=args.dtype, parity=parity)
+        desc = f"D2Q9 MRT lid-driven cavity {n}^2 (bounce-back walls, moving lid)"
     else:
         sim = Simulation(W.cavity3d(n=n), dtype=args.dtype)
         desc = f"D3Q19 MRT lid-driven cube {n}^3 (bounce-back on every wall, moving lid)"
+    sim.module.call(sim.module.lib.lbm_scheme_set_step_variant(args.step_variant))
     grid = list(sim.domain.shape_in)
     nodes = int(np.prod(grid))
     buf_bytes = sim._lat.elements * BYTES_PER_VALUE[args.dtype]

@@ -404,6 +404,16 @@ int lbm_one_time_step(const void* f, void* fnew, const lbm_lattice* lat, const d
 int lbm_one_time_step_periodic(const void* f, void* fnew, const lbm_lattice* lat,
                                const double* prm, void* stream);
 
+/* Step kernel choice of this module: 1 runs periodic steps of 16-bit
+ * storage in the staged kernel where the rows allow it (bulk copies of each
+ * pulled row into shared memory on the TMA unit, ahead of the compute), 0
+ * (default) the direct-load kernels; both give the same results bit for bit.
+ * No reference counterpart. */
+int lbm_scheme_set_step_variant(int32_t variant);
+/* Number of bounded waits of this module's kernels that gave up (0 in a
+ * healthy run; a kernel whose wait times out leaves without completing). */
+int lbm_scheme_wait_timeouts(uint32_t* count);
+
 /* Periodic step with the learned collision closure (no reference
  * counterpart): after the relaxation, the non-conserved moments k >= nconsm
  * receive corr_j = y_j * sig_out[j] + mu_out[j], y = MLP((m - mu_in) * isig_in)

@@ -195,6 +195,57 @@ inline int check_lattice(const lbm_lattice* l, const char* who) {
   return LBM_OK;
 }
 
+// ---------------------------------------------------------------- async copies
+// Bulk copies global -> shared on the TMA unit (cp.async.bulk) completing on
+// an mbarrier, and the mbarrier operations around them.  Every wait is
+// bounded in time: after kWaitCycles SM clocks it gives up and returns false
+// (the caller records the timeout and leaves), so no kernel can spin forever.
+constexpr long long kWaitCycles = 4000000000LL;  // about two seconds at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+// the initialised barriers become visible to the async proxy (the copy engine)
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// wait for the phase of the given parity to complete; false after the time bound
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_test(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
+}
+// `bytes` (a multiple of 16) from global src to shared dst, both 16-byte aligned
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
 // Element offset of halo coordinates (i0, i1, i2) of population 0.
 __host__ __device__ __forceinline__ long long node_offset(const Geo& g, int i0, int i1, int i2) {
   return g.origin + (long long)i0 * g.stride[0] + (long long)i1 * g.stride[1] +

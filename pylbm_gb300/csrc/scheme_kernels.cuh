@@ -316,6 +316,138 @@ __global__ void __launch_bounds__(LBM_BLOCK, LBM_PAIRS_MIN_BLOCKS) k_step_period
   for (int p = 0; p < kPrm; ++p) prm[p] = lbm::F2((float)a.prm[p]);
   step_pair(f, fnew, a.g, prm, i0, i1, i2, z, nL);
 }
+
+// ---------------------------------------------------------------------------
+// Staged periodic step (16-bit storage, two nodes per thread).  A persistent
+// block owns a sequence of interior rows (all axes but the contiguous one);
+// for each row one producer thread issues Q bulk copies on the TMA unit --
+// for population k, the interior row the pull reads (the row at x - v_k,
+// wrapped periodically along the outer axes) -- into one of kStages shared
+// buffers, completing on that stage's "full" mbarrier.  Four consumer warps
+// wait on it, take each node's Q values from shared memory (the wrap along
+// the contiguous axis is an index into the staged row), collide two nodes
+// per thread and store them, then release the stage on its "empty" mbarrier.
+// The copies of the next stages are in flight while a row is computed, with
+// no registers held for them: the one-node-per-load kernels are limited by
+// the loads a thread can keep in flight at the occupancy its registers allow.
+// Every wait is bounded (lbm::mbar_wait); a timed-out wait is counted in
+// lbm_wait_timeouts and the block leaves after its copies have landed.
+constexpr int kStages = 4;
+constexpr int kConsumers = 4;  // warps
+constexpr int kStagedThreads = 32 * (1 + kConsumers);
+
+__device__ unsigned int lbm_wait_timeouts;
+
+__device__ __forceinline__ void staged_row_coords(const Geo& g, int r, int& i0, int& i1) {
+#if LBM_DIM == 3
+  i0 = r / g.n[1];
+  i1 = r - i0 * g.n[1];
+#else
+  i0 = r;
+  i1 = 0;
+#endif
+}
+
+// interior coordinate c shifted by -v and wrapped into [0, n)
+__device__ __forceinline__ int wrap_back(int c, int v, int n) {
+  int j = c - v;
+  return j < 0 ? j + n : (j >= n ? j - n : j);
+}
+
+// the two pulled values of nodes (z, z+1) from a staged row of nL values
+__device__ __forceinline__ lbm::F2 staged_pair(const S* __restrict__ row, int vl, int z, int nL) {
+  if (vl == 0) {
+    const float2 w = Pair<S>::load(row + z);
+    return lbm::F2(w.x, w.y);
+  }
+  const int a = wrap_back(z, vl, nL), b = wrap_back(z + 1, vl, nL);
+  return lbm::F2(Pair<S>::one(row + a), Pair<S>::one(row + b));
+}
+
+__global__ void __launch_bounds__(kStagedThreads) k_step_periodic_staged(const S* __restrict__ f,
+                                                                        S* __restrict__ fnew, StepArgs a) {
+  constexpr int L = LBM_DIM - 1;
+  extern __shared__ __align__(128) unsigned char staged_smem[];
+  const Geo& g = a.g;
+  const int nL = g.n[L];
+  const int rows = LBM_DIM == 3 ? g.n[0] * g.n[1] : g.n[0];
+  const uint32_t row_bytes = (uint32_t)nL * sizeof(S);
+  S* buf = reinterpret_cast<S*>(staged_smem);
+  uint64_t* full = reinterpret_cast<uint64_t*>(staged_smem + (size_t)kStages * LBM_Q * row_bytes);
+  uint64_t* empty = full + kStages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      lbm::mbar_init(&full[s], 1);
+      lbm::mbar_init(&empty[s], kConsumers);
+    }
+    lbm::mbar_init_fence();
+  }
+  __syncthreads();
+  if (warp == 0) {
+    if (lane != 0) return;
+    // producer: the Q source rows of every row this block owns
+    int it = 0;
+    bool ok = true;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x, ++it) {
+      const int s = it % kStages;
+      if (it >= kStages && !lbm::mbar_wait(&empty[s], ((it / kStages) - 1) & 1)) {
+        ok = false;
+        break;
+      }
+      lbm::mbar_expect_tx(&full[s], LBM_Q * row_bytes);
+      int x0, x1;
+      staged_row_coords(g, r, x0, x1);
+#define LBM_STAGE_ROW(k, vx, vy, vz)                                                                  \
+  {                                                                                                   \
+    const int s0 = wrap_back(x0, LBM_DIM == 3 ? (vx) : (LBM_DIM == 2 ? (vx) : 0), g.n[0]) + g.h[0];   \
+    const int s1 = LBM_DIM == 3 ? wrap_back(x1, (vy), g.n[1]) + g.h[1] : 0;                           \
+    const S* src = f + (long long)(k) * g.vstride + lbm::node_offset(g, s0, s1, 0) + g.h[L];          \
+    lbm::bulk_load(buf + ((size_t)s * LBM_Q + (k)) * nL, src, row_bytes, &full[s]);                   \
+  }
+      LBM_FOR_EACH_V(LBM_STAGE_ROW)
+#undef LBM_STAGE_ROW
+    }
+    if (!ok) atomicAdd(&lbm_wait_timeouts, 1u);
+    // the copies still in flight land before the block's shared memory goes away
+    for (int j = it - 1; j >= 0 && j >= it - kStages; --j)
+      if (!lbm::mbar_wait(&full[j % kStages], (j / kStages) & 1)) {
+        atomicAdd(&lbm_wait_timeouts, 1u);
+        break;
+      }
+    return;
+  }
+  // consumers
+  lbm::F2 prm[kPrm];
+#pragma unroll
+  for (int p = 0; p < kPrm; ++p) prm[p] = lbm::F2((float)a.prm[p]);
+  const int t = threadIdx.x - 32;
+  int it = 0;
+  for (int r = blockIdx.x; r < rows; r += gridDim.x, ++it) {
+    const int s = it % kStages;
+    if (!lbm::mbar_wait(&full[s], (it / kStages) & 1)) {
+      if (lane == 0) atomicAdd(&lbm_wait_timeouts, 1u);
+      break;
+    }
+    int x0, x1;
+    staged_row_coords(g, r, x0, x1);
+    const S* stage = buf + (size_t)s * LBM_Q * nL;
+    for (int z = 2 * t; z < nL; z += 2 * 32 * kConsumers) {
+      lbm::F2 gv[LBM_Q];
+#define LBM_PULL_STAGED(k, vx, vy, vz) gv[k] = staged_pair(stage + (size_t)(k) * nL, LBM_VL(vx, vy, vz), z, nL);
+      LBM_FOR_EACH_V(LBM_PULL_STAGED)
+#undef LBM_PULL_STAGED
+#if LBM_DIM == 3
+      collide_store_pairs(fnew, g, prm, x0 + g.h[0], x1 + g.h[1], z + g.h[2], gv);
+#else
+      collide_store_pairs(fnew, g, prm, x0 + g.h[0], z + g.h[1], 0, gv);
+#endif
+    }
+    __syncwarp();
+    if (lane == 0) lbm::mbar_arrive(&empty[s]);
+  }
+}
+
 #else
 #define LBM_HAS_PAIRS 0
 #endif
@@ -745,6 +877,24 @@ inline bool pairs_fit(const lbm_lattice& l, const void* f, const void* fnew) {
   return ((uintptr_t)f % 4 == 0) && ((uintptr_t)fnew % 4 == 0);
 }
 
+#if LBM_HAS_PAIRS
+// the staged step applies: 2D or 3D rows whose bytes and starts suit bulk copies
+inline bool staged_fits(const lbm_lattice& l, const void* f, const void* fnew) {
+  const int L = LBM_DIM - 1;
+  if (LBM_DIM < 2 || !pairs_fit(l, f, fnew)) return false;
+  const long long es = (long long)sizeof(S);
+  if ((l.n[L] * es) % 16 || l.n[L] > 1024) return false;  // row bytes: multiple of 16, stage within shared memory
+  if (((l.origin + l.halo[L]) * es) % 16 || (l.vstride * es) % 16) return false;
+  for (int d = 0; d < L; ++d)
+    if ((l.stride[d] * es) % 16) return false;
+  return ((uintptr_t)f % 16 == 0);
+}
+
+inline size_t staged_smem_bytes(const lbm_lattice& l) {
+  return (size_t)kStages * LBM_Q * l.n[LBM_DIM - 1] * sizeof(S) + 2 * kStages * sizeof(uint64_t);
+}
+#endif
+
 inline StepArgs make_step_args(const lbm_lattice& l, const double* prm) {
   StepArgs a;
   a.g = lbm::make_geo(l);
@@ -776,6 +926,27 @@ int lbm_scheme_describe(int32_t* nv, int32_t* dim, int32_t* nprm, int32_t* stora
   return LBM_OK;
 }
 
+// 0 (default): the direct-load kernels; 1: periodic 16-bit steps use the
+// staged kernel where the rows fit
+static int g_step_variant = 0;
+
+int lbm_scheme_set_step_variant(int32_t variant) {
+  if (variant < 0 || variant > 1) return lbm::fail(LBM_ERR_ARG, "lbm_scheme_set_step_variant: %d", variant);
+  g_step_variant = variant;
+  return LBM_OK;
+}
+
+int lbm_scheme_wait_timeouts(uint32_t* count) {
+  if (!count) return lbm::fail(LBM_ERR_ARG, "lbm_scheme_wait_timeouts: NULL");
+#if LBM_HAS_PAIRS
+  return lbm::cuda_check(cudaMemcpyFromSymbol(count, lbm_scheme::lbm_wait_timeouts, sizeof(uint32_t)),
+                         "lbm_scheme_wait_timeouts");
+#else
+  *count = 0;
+  return LBM_OK;
+#endif
+}
+
 static int step_common(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, void* stream,
                        bool periodic, const char* who) {
   using namespace lbm_scheme;
@@ -788,6 +959,34 @@ static int step_common(const void* f, void* fnew, const lbm_lattice* lat, const 
   dim3 grid = node_grid(*lat, false);
   cudaStream_t s = (cudaStream_t)stream;
 #if LBM_HAS_PAIRS
+  if (periodic && g_step_variant == 1 && staged_fits(*lat, f, fnew)) {
+    const size_t smem = staged_smem_bytes(*lat);
+    // shared-memory limit and resident blocks per SM, looked up once per device and size
+    static int cache_dev = -1, cache_blocks = 0;
+    static size_t cache_smem = 0;
+    int dev = 0;
+    rc = lbm::cuda_check(cudaGetDevice(&dev), who);
+    if (rc) return rc;
+    if (dev != cache_dev || smem != cache_smem) {
+      int sms = 0, per_sm = 0;
+      rc = lbm::cuda_check(cudaFuncSetAttribute(k_step_periodic_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem),
+                           who);
+      if (!rc) rc = lbm::cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), who);
+      if (!rc)
+        rc = lbm::cuda_check(
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_periodic_staged, kStagedThreads, smem),
+            who);
+      if (rc) return rc;
+      cache_dev = dev;
+      cache_smem = smem;
+      cache_blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    const int rows = LBM_DIM == 3 ? lat->n[0] * lat->n[1] : lat->n[0];
+    const int blocks = cache_blocks < rows ? cache_blocks : rows;
+    k_step_periodic_staged<<<blocks, kStagedThreads, smem, s>>>((const S*)f, (S*)fnew, a);
+    return lbm::launch_check(who);
+  }
   if (pairs_fit(*lat, f, fnew)) {
     grid.x = (unsigned)((lat->n[LBM_DIM - 1] / 2 + LBM_BLOCK - 1) / LBM_BLOCK);
     if (periodic)

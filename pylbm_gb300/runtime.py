@@ -454,6 +454,8 @@ class SchemeModule:
         _sig(lib, "lbm_equilibrium", I32, [P, LP, P, P])
         _sig(lib, "lbm_relaxation", I32, [P, LP, P, P])
         _sig(lib, "lbm_source_term", I32, [P, LP, P, P])
+        _sig(lib, "lbm_scheme_set_step_variant", I32, [I32])
+        _sig(lib, "lbm_scheme_wait_timeouts", I32, [ctypes.POINTER(ctypes.c_uint32)])
         _sig(lib, "lbm_ensemble_step", I32, [P, P, P, I32, I32, I32, I32, I32, P])
         _sig(lib, "lbm_ensemble_step_pairs", I32, [P, P, P, I32, I32, I32, I32, I32, P])
         _sig(lib, "lbm_one_time_step_periodic_closure", I32, [P, P, LP, P, P, P, P, P, P, I32, P])
