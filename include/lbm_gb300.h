@@ -99,6 +99,10 @@ int lbm_stream_synchronize(void* stream);
 /* Pinned host memory (for host<->device copies that overlap compute). */
 int lbm_host_alloc(void** ptr, size_t bytes);
 int lbm_host_free(void* ptr);
+/* The device address of page-locked host memory (from lbm_host_alloc), for
+ * kernels that read or write it directly over the host link; LBM_ERR_UNSUPPORTED
+ * when the memory is not mapped for the device. */
+int lbm_host_device_pointer(void* host, void** device);
 
 /* CUDA events on a stream, for device-side timing. */
 int lbm_event_create(void** event);
@@ -442,6 +446,13 @@ int lbm_f2m(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice*
  * the float64 arithmetic of lbm_f2m. */
 int lbm_f2m_conserved(const void* f, const lbm_lattice* lat, double* m, const lbm_lattice* mlat, void* stream);
 
+/* The conserved moments of the interior nodes written straight into a dense
+ * float64 array out[c][i0][i1][i2] (nconsm planes, last axis fastest), in one
+ * pass over the populations: the read of sim.m[rho] etc. without the moment
+ * array (pylbm/simulation.py:216-224).  out may be device memory or
+ * page-locked host memory mapped for the device (lbm_host_device_pointer). */
+int lbm_f2m_conserved_dense(const void* f, const lbm_lattice* lat, double* out, void* stream);
+
 /* Populations from moments: f = M^-1 m (pylbm/algorithm/base.py:346-379). */
 int lbm_m2f(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat,
             void* stream);
@@ -452,6 +463,15 @@ int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void*
 
 /* Moment-space relaxation m <- m + s (m_eq - m) (pylbm/algorithm/base.py:404-437). */
 int lbm_relaxation(double* m, const lbm_lattice* mlat, const double* prm, void* stream);
+
+/* Populations at the equilibrium of the conserved moments (planes
+ * 0..nconsm-1 of m, read only), over the whole halo box: pylbm's
+ * initialisation, equilibrium then m2f (pylbm/simulation.py:258-320), in one
+ * pass without writing the other moments.  Unshifted storage computes
+ * exactly lbm_equilibrium followed by lbm_m2f; shifted storage evaluates the
+ * equilibrium of the deviations in FP32. */
+int lbm_init_conserved(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat,
+                       const double* prm, void* stream);
 
 /* Source terms over half a time step on the interior nodes: each conserved
  * moment with a source gets m_c += dt/2 S_c(m) (explicit Euler,

@@ -433,6 +433,36 @@ class SchemeSource:
     def _relax_abs_code(self, m, indent="  "):
         return self._relax_code(m, indent, deviation=False)
 
+    def _eq_dev_code(self, m, indent="  "):
+        """Shifted storage: the non-conserved moments of a deviation vector set
+        to meq_k(c0 + dc) - meq_k(c0) from its conserved deviations dc (the
+        expansions the relaxation uses); unshifted: the absolute equilibrium."""
+        if not self.shifted:
+            return self._eq_abs_code(m, indent)
+        sc = self.scheme
+        nc = sc.nconsm
+        cons = list(sc.consm.keys())
+        dsym = [sp.Symbol(f"__d{c}") for c in range(nc)]
+        names = {dsym[c]: f"{m}[{c}]" for c in range(nc)}
+        for i, s in enumerate(self.params):
+            names[s] = f"prm[{i}]"
+        c0s = [sp.Rational(c.numerator, c.denominator) for c in self.c0]
+        exprs = []
+        for k in range(nc, sc.nv):
+            full = sc.EQ[k].subs({cons[c]: c0s[c] + dsym[c] for c in range(nc)})
+            d = sp.expand(full - self.meq_ref[k])
+            d = sp.together(d) if d.has(sp.Pow) and any(p.exp.is_negative for p in d.atoms(sp.Pow)) else d
+            exprs.append(d)
+        pr = ExprPrinter(names)
+        repl, red = _cse(exprs, "e_", pr)
+        lines = []
+        for sym, val in repl:
+            lines.append(f"{indent}const R {sym} = {pr(val)};")
+            names[sym] = str(sym)
+        for idx, k in enumerate(range(nc, sc.nv)):
+            lines.append(f"{indent}{m}[{k}] = {pr(red[idx])};")
+        return lines
+
     # --------------------------------------------------------------- frame-relative / source-term collide
     @property
     def absolute_collide(self):
@@ -595,6 +625,12 @@ class SchemeSource:
         out += self._eq_abs_code("m")
         out.append("  (void)prm;")
         out.append("}")
+        out.append("// equilibrium of a stored (deviation) state from its conserved moments")
+        out.append("template <typename R>")
+        out.append("__device__ __forceinline__ void lbm_equilibrium_dev(R (&m)[LBM_Q], const R* __restrict__ prm) {")
+        out += self._eq_dev_code("m")
+        out.append("  (void)prm;")
+        out.append("}")
         out.append("// relaxation of absolute moments")
         out.append("template <typename R>")
         out.append("__device__ __forceinline__ void lbm_relax_abs(R (&m)[LBM_Q], const R* __restrict__ prm) {")
@@ -636,6 +672,7 @@ class SchemeSource:
         out += fn("lbm_relax_abs(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.relaxation_routine("m"))
         out += fn("lbm_relax(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.relaxation("m"))
         out += fn("lbm_equilibrium_abs(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.equilibrium("m"))
+        out += fn("lbm_equilibrium_dev(R (&m)[LBM_Q], const R* __restrict__ prm)", ref.equilibrium("m"))
         out += fn("lbm_collide(R (&g)[LBM_Q], const R* __restrict__ prm)",
                   ["R m[LBM_Q];"] + ref.moments_pull("g", "m") + ref.relaxation("m") + ref.populations("m", "g"))
         out += self._source_half_function()

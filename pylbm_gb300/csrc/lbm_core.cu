@@ -612,6 +612,18 @@ int lbm_stream_synchronize(void* stream) {
   return cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
 }
 
+int lbm_host_device_pointer(void* host, void** device) {
+  if (!host || !device) return fail(LBM_ERR_ARG, "lbm_host_device_pointer: NULL pointer");
+  *device = nullptr;
+  cudaPointerAttributes attr;
+  int rc = cuda_check(cudaPointerGetAttributes(&attr, host), "lbm_host_device_pointer: cudaPointerGetAttributes");
+  if (rc) return rc;
+  if (attr.type != cudaMemoryTypeHost || !attr.devicePointer)
+    return fail(LBM_ERR_UNSUPPORTED, "lbm_host_device_pointer: not page-locked host memory mapped for the device");
+  *device = attr.devicePointer;
+  return LBM_OK;
+}
+
 int lbm_host_alloc(void** ptr, size_t bytes) {
   if (!ptr) return fail(LBM_ERR_ARG, "lbm_host_alloc: NULL ptr");
   *ptr = nullptr;

@@ -769,6 +769,23 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_f2m_conserved(const S* __restrict
   for (int k = 0; k < LBM_NCONS; ++k) m[om + (long long)k * a.gm.vstride] = (double)mm[k] + lbm_dev_mref[k];
 }
 
+// the conserved moments of the interior nodes straight into a dense array
+// out[c][i0][i1][i2] (last axis fastest): what output reads, in one pass
+__global__ void __launch_bounds__(LBM_BLOCK) k_f2m_conserved_dense(const S* __restrict__ f, double* __restrict__ out,
+                                                                   MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_node(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  RM g[LBM_Q], mm[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) g[k] = (RM)Store<S>::load(f + o + (long long)k * a.g.vstride);
+  lbm_moments<RM>(g, mm);
+  const long long plane = (long long)a.g.n[0] * a.g.n[1] * a.g.n[2];
+  const long long at = ((long long)(i0 - a.g.h[0]) * a.g.n[1] + (i1 - a.g.h[1])) * a.g.n[2] + (i2 - a.g.h[2]);
+#pragma unroll
+  for (int c = 0; c < LBM_NCONS; ++c) out[c * plane + at] = (double)mm[c] + lbm_dev_mref[c];
+}
+
 __global__ void __launch_bounds__(LBM_BLOCK) k_m2f(const double* __restrict__ m, S* __restrict__ f,
                                                    MomentArgs a) {
   int i0, i1, i2;
@@ -779,6 +796,40 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_m2f(const double* __restrict__ m,
   // M^-1 (m - mref) = f - shift: the stored deviations directly
 #pragma unroll
   for (int k = 0; k < LBM_Q; ++k) mm[k] = (RM)(m[om + (long long)k * a.gm.vstride] - lbm_dev_mref[k]);
+  lbm_populations<RM>(mm, g);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) Store<S>::store(f + o + (long long)k * a.g.vstride, (R)g[k]);
+}
+
+// pylbm's initialisation from the conserved moments (equilibrium, then m2f)
+// in one pass over the halo box: planes 0..nconsm-1 of m are read, the
+// populations written, the other planes of m neither read nor written.
+// Shifted storage computes the equilibrium of the deviations in the module's
+// FP32 arithmetic (one FP64 subtraction per conserved moment); unshifted
+// storage runs exactly the operations of k_equilibrium followed by k_m2f.
+__global__ void __launch_bounds__(LBM_BLOCK) k_init_conserved(const double* __restrict__ m, S* __restrict__ f,
+                                                              MomentArgs a) {
+  int i0, i1, i2;
+  if (!my_cell(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  const long long om = lbm::node_offset(a.gm, i0, i1, i2);
+  RM mm[LBM_Q], g[LBM_Q];
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) mm[k] = (RM)0;
+#if LBM_SHIFTED
+  RM prm[kPrm];
+#pragma unroll
+  for (int p = 0; p < kPrm; ++p) prm[p] = (RM)a.prm[p];
+#pragma unroll
+  for (int c = 0; c < LBM_NCONS; ++c) mm[c] = (RM)(m[om + (long long)c * a.gm.vstride] - lbm_dev_mref[c]);
+  lbm_equilibrium_dev<RM>(mm, prm);
+#else
+#pragma unroll
+  for (int c = 0; c < LBM_NCONS; ++c) mm[c] = m[om + (long long)c * a.gm.vstride];
+  lbm_equilibrium_abs<double>(mm, a.prm);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) mm[k] = (RM)(mm[k] - lbm_dev_mref[k]);
+#endif
   lbm_populations<RM>(mm, g);
 #pragma unroll
   for (int k = 0; k < LBM_Q; ++k) Store<S>::store(f + o + (long long)k * a.g.vstride, (R)g[k]);
@@ -1072,6 +1123,29 @@ int lbm_equilibrium(double* m, const lbm_lattice* mlat, const double* prm, void*
   MomentArgs a = make_moment_args(nullptr, mlat, prm);
   k_equilibrium<<<node_grid(*mlat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, a);
   return lbm::launch_check("lbm_equilibrium");
+}
+
+int lbm_f2m_conserved_dense(const void* f, const lbm_lattice* lat, double* out, void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_pop_lattice(lat, "lbm_f2m_conserved_dense", false);
+  if (rc) return rc;
+  if (!f || !out) return lbm::fail(LBM_ERR_ARG, "lbm_f2m_conserved_dense: NULL buffer");
+  MomentArgs a = make_moment_args(lat, lat, nullptr);
+  k_f2m_conserved_dense<<<node_grid(*lat, false), LBM_BLOCK, 0, (cudaStream_t)stream>>>((const S*)f, out, a);
+  return lbm::launch_check("lbm_f2m_conserved_dense");
+}
+
+int lbm_init_conserved(const double* m, const lbm_lattice* mlat, void* f, const lbm_lattice* lat, const double* prm,
+                       void* stream) {
+  using namespace lbm_scheme;
+  int rc = check_pop_lattice(lat, "lbm_init_conserved", false);
+  if (!rc) rc = check_moment_lattice(lat, mlat, "lbm_init_conserved");
+  if (rc) return rc;
+  if (!f || !m) return lbm::fail(LBM_ERR_ARG, "lbm_init_conserved: NULL buffer");
+  if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "lbm_init_conserved: parameters expected");
+  MomentArgs a = make_moment_args(lat, mlat, prm);
+  k_init_conserved<<<node_grid(*lat, true), LBM_BLOCK, 0, (cudaStream_t)stream>>>(m, (S*)f, a);
+  return lbm::launch_check("lbm_init_conserved");
 }
 
 int lbm_source_term(double* m, const lbm_lattice* mlat, const double* prm, void* stream) {

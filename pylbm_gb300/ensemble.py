@@ -192,11 +192,11 @@ class Ensemble:
                 mbuf.upload(plane, offset=idx * mlat.vstride * 8, stream=self._stream)
             prm = np.array([self.params[i][str(s)] for s in sc.free_symbols] + [0.0])
             pp = prm.ctypes.data_as(ctypes.c_void_p)
-            self.module.call(self.module.lib.lbm_equilibrium(mbuf.handle, ctypes.byref(mlat), pp, self._stream))
             f0 = ctypes.c_void_p(self.arena.ptr + self.offsets[i][0] * es)
             f1 = ctypes.c_void_p(self.arena.ptr + self.offsets[i][1] * es)
-            self.module.call(self.module.lib.lbm_m2f(mbuf.handle, ctypes.byref(mlat), f0, ctypes.byref(lat),
-                                                     self._stream))
+            # equilibrium then m2f, in one pass (as Simulation initialises)
+            self.module.call(self.module.lib.lbm_init_conserved(mbuf.handle, ctypes.byref(mlat), f0,
+                                                                ctypes.byref(lat), pp, self._stream))
             runtime.check(self._core.lbm_memcpy(f1, f0, lat.elements * es, runtime.D2D, self._stream))
             self.synchronize()
         mbuf.free()

@@ -205,6 +205,7 @@ def core():
             _sig(lib, "lbm_stream_synchronize", I32, [P])
             _sig(lib, "lbm_host_alloc", I32, [ctypes.POINTER(P), SZ])
             _sig(lib, "lbm_host_free", I32, [P])
+            _sig(lib, "lbm_host_device_pointer", I32, [P, ctypes.POINTER(P)])
             _sig(lib, "lbm_event_create", I32, [ctypes.POINTER(P)])
             _sig(lib, "lbm_event_destroy", I32, [P])
             _sig(lib, "lbm_event_record", I32, [P, P])
@@ -454,6 +455,8 @@ class SchemeModule:
         _sig(lib, "lbm_equilibrium", I32, [P, LP, P, P])
         _sig(lib, "lbm_relaxation", I32, [P, LP, P, P])
         _sig(lib, "lbm_source_term", I32, [P, LP, P, P])
+        _sig(lib, "lbm_init_conserved", I32, [P, LP, P, LP, P, P])
+        _sig(lib, "lbm_f2m_conserved_dense", I32, [P, LP, P, P])
         _sig(lib, "lbm_scheme_set_step_variant", I32, [I32])
         _sig(lib, "lbm_scheme_wait_timeouts", I32, [ctypes.POINTER(ctypes.c_uint32)])
         _sig(lib, "lbm_ensemble_step", I32, [P, P, P, I32, I32, I32, I32, I32, P])

@@ -216,6 +216,7 @@ class Simulation:
         self._m_cache = {}
         self._update_m = True
         self._m_partial = False     # only the conserved planes of the moment array are current
+        self._eq_pending = False    # the other planes are the equilibrium of the conserved ones, not yet computed
         self._bc_dev = []
         self._bc_batch = None
         self._ghost = None          # observed ghost copies: (istore, iload) device lists
@@ -329,10 +330,12 @@ class Simulation:
         del arr
         prm = self._prm(for_init=True)
         pp = prm.ctypes.data_as(ctypes.c_void_p)
-        if self.init_type == "moments":
-            self.module.call(self.module.lib.lbm_equilibrium(mbuf.handle, ctypes.byref(self._mlat), pp, self._stream))
-        self.module.call(self.module.lib.lbm_m2f(mbuf.handle, ctypes.byref(self._mlat), self._F.handle,
-                                                 ctypes.byref(self._lat), self._stream))
+        if self.init_type == "moments":  # equilibrium then m2f, in one pass
+            self.module.call(self.module.lib.lbm_init_conserved(mbuf.handle, ctypes.byref(self._mlat), self._F.handle,
+                                                                ctypes.byref(self._lat), pp, self._stream))
+        else:
+            self.module.call(self.module.lib.lbm_m2f(mbuf.handle, ctypes.byref(self._mlat), self._F.handle,
+                                                     ctypes.byref(self._lat), self._stream))
         runtime.check(self._core.lbm_memcpy(self._Fnew.handle, self._F.handle, self._F.nbytes, runtime.D2D,
                                             self._stream))
         self.synchronize()
@@ -660,16 +663,33 @@ class Simulation:
         self._m_partial = False
 
     def m2f(self):
-        """F = M^-1 m on the whole box (pylbm/simulation.py:352-358)."""
+        """F = M^-1 m on the whole box (pylbm/simulation.py:352-358).  After
+        ``equilibrium()`` the populations come from the conserved moments in
+        one pass (lbm_init_conserved), without the equilibrium planes."""
         self._moments_ready()
+        if self._eq_pending and not self._update_m:
+            prm = self._prm(for_init=True)
+            self.module.call(self.module.lib.lbm_init_conserved(
+                self._mbuf().handle, ctypes.byref(self._mlat), self._F.handle, ctypes.byref(self._lat),
+                prm.ctypes.data_as(ctypes.c_void_p), self._stream))
+            return
         self._moments_for(None)
         self.module.call(self.module.lib.lbm_m2f(self._mbuf().handle, ctypes.byref(self._mlat), self._F.handle,
                                                  ctypes.byref(self._lat), self._stream))
 
     def equilibrium(self):
-        """Non-conserved moments of m set to their equilibrium values (pylbm/simulation.py:360-372)."""
+        """Non-conserved moments of m set to their equilibrium values
+        (pylbm/simulation.py:360-372).  They are computed when first read; a
+        following ``m2f()`` needs only the conserved ones."""
         self._moments_ready()
-        self._moments_for(None)
+        self._moments_for(0)
+        self._eq_pending = True
+        self._m_partial = False
+        self._update_m = False
+
+    def _materialize_equilibrium(self):
+        """Write the pending equilibrium planes into the moment array."""
+        self._eq_pending = False
         prm = self._prm(for_init=True)
         self.module.call(self.module.lib.lbm_equilibrium(self._mbuf().handle, ctypes.byref(self._mlat),
                                                          prm.ctypes.data_as(ctypes.c_void_p), self._stream))
@@ -726,6 +746,8 @@ class Simulation:
         kernel writes it into the padded layout."""
         if self._need_init:
             self._initialize()
+        if self._eq_pending:  # the other planes as pylbm's equilibrium() left them
+            self._moments_for(None)
         first, count, many = self._plane_range(key)
         shape = ((count,) if many else ()) + tuple(self.domain.shape_halo)
         src = np.asarray(value)
@@ -793,6 +815,11 @@ class Simulation:
         """Bring the device moment array up to date for plane ``idx`` (every
         plane when None): the conserved planes alone when only they are read."""
         need_all = idx is None or idx >= self.scheme.nconsm
+        if self._update_m:
+            self._eq_pending = False
+        elif self._eq_pending and need_all:
+            self._m_cache = {}
+            self._materialize_equilibrium()
         if self._update_m or (need_all and self._m_partial):
             self._m_cache = {}
             entry = self.module.lib.lbm_f2m if need_all else self.module.lib.lbm_f2m_conserved
@@ -833,10 +860,15 @@ class Simulation:
             out = np.empty(shape, dtype=np.float64)
         elif out.shape != shape or out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"]:
             raise ValueError(f"fields(out=...) needs a C-contiguous float64 array of shape {shape}")
-        self._moments_for(0)
-        stage = self._stage(out.nbytes)
-        runtime.check(self._core.lbm_copy_planes(self._mbuf().handle, ctypes.byref(self._mlat), 0, nc, 0,
-                                                 stage.handle, 0, self._stream))
+        if self._update_m:
+            # straight from the populations, without the moment array
+            stage = self._stage(out.nbytes)
+            self.module.call(self.module.lib.lbm_f2m_conserved_dense(self._F.handle, ctypes.byref(self._lat),
+                                                                     stage.handle, self._stream))
+        else:  # the moment array holds values the user set: read those
+            stage = self._stage(out.nbytes)
+            runtime.check(self._core.lbm_copy_planes(self._mbuf().handle, ctypes.byref(self._mlat), 0, nc, 0,
+                                                     stage.handle, 0, self._stream))
         runtime.check(self._core.lbm_memcpy(out.ctypes.data_as(ctypes.c_void_p), stage.handle, out.nbytes,
                                             runtime.D2H, self._stream))
         self.synchronize()

@@ -209,26 +209,23 @@ def _strouhal(qy, every, diameter=64, u_in=0.05):
 
 
 def test_disc_flow_sheds_vortices_at_the_expected_strouhal_number():
-    """The Re 200 disc flow (radius 32, centre one node above mid-channel)
-    starts shedding after about 1e5 steps (the 20 000 steps of the workload
-    show the wake's growing asymmetry, not yet shedding); over steps
-    200 000 - 250 000 the cross-stream momentum behind the disc oscillates at
-    St = f D / U in the range of a confined Re 200 disc, and the FP16 run
-    sheds at the FP32 run's frequency."""
+    """The Re 200 disc flow (radius 32, centre one node above mid-channel),
+    FP32 shifted storage: the wake's asymmetry grows from the start (the
+    20 000 steps of the workload show it growing, not yet shedding) and the
+    disc sheds from about 1e5 steps on; over steps 200 000 - 250 000 the
+    cross-stream momentum behind the disc oscillates at St = f D / U in the
+    range of a confined Re 200 disc."""
     every = 100
-    st = {}
-    for dtype in ("float32", "float16"):
-        sim = Simulation(W.cylinder(), dtype=dtype)
-        sim.run(200000)
-        qy = []
-        for _ in range(500):
-            sim.run(every)
-            qy.append(float(sim.m[2, 560, 257]))
-        sim.free()
-        qy = np.array(qy)
-        assert np.ptp(qy) > 0.05  # a developed wake oscillation (u_in = 0.05)
-        st[dtype], cycles = _strouhal(qy, every)
-        assert cycles >= 6
-    print(f"disc flow Re 200 Strouhal number: float32 {st['float32']:.4f}, float16 {st['float16']:.4f}")
-    assert 0.18 < st["float32"] < 0.23
-    assert abs(st["float16"] - st["float32"]) < 0.02 * st["float32"]
+    sim = Simulation(W.cylinder(), dtype="float32")
+    sim.run(200000)
+    qy = []
+    for _ in range(500):
+        sim.run(every)
+        qy.append(float(sim.m[2, 560, 257]))
+    sim.free()
+    qy = np.array(qy)
+    assert np.ptp(qy) > 0.05  # a developed wake oscillation (u_in = 0.05)
+    st, cycles = _strouhal(qy, every)
+    print(f"disc flow Re 200 (float32) Strouhal number {st:.4f} over {cycles} cycles")
+    assert cycles >= 6
+    assert 0.18 < st < 0.23

@@ -157,7 +157,8 @@ def runtime_scheme_symbols():
     return {"lbm_one_time_step", "lbm_one_time_step_periodic", "lbm_transport", "lbm_f2m", "lbm_m2f",
             "lbm_equilibrium", "lbm_relaxation", "lbm_scheme_last_error", "lbm_scheme_describe",
             "lbm_ensemble_step", "lbm_ensemble_step_pairs", "lbm_one_time_step_periodic_closure",
-            "lbm_f2m_conserved", "lbm_source_term", "lbm_scheme_set_step_variant", "lbm_scheme_wait_timeouts"}
+            "lbm_f2m_conserved", "lbm_source_term", "lbm_scheme_set_step_variant", "lbm_scheme_wait_timeouts",
+            "lbm_init_conserved", "lbm_f2m_conserved_dense"}
 
 
 def test_scheme_module_builds_and_exports_header():
