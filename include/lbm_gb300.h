@@ -408,6 +408,20 @@ int lbm_one_time_step(const void* f, void* fnew, const lbm_lattice* lat, const d
 int lbm_one_time_step_periodic(const void* f, void* fnew, const lbm_lattice* lat,
                                const double* prm, void* stream);
 
+/* One step on a box whose boundary links are all bounce-back links of its
+ * walls (pylbm/boundary.py:400-469 applied in the pull): a wall node pulling
+ * population k from beyond a wall takes f_k'(x) + table[k * 27 + sig] (k' =
+ * sym[k], the opposite population; sig = 9 (o0+1) + 3 (o1+1) + (o2+1), o_d =
+ * -1 / 0 / +1 where the source lies below / inside / above the interior along
+ * axis d), rounded through the storage type: the same populations as the
+ * boundary launch (lbm_boundary_batch, bounce-back links) followed by
+ * lbm_one_time_step, bit for bit, in one launch that neither reads nor writes
+ * ghost slots.  table: nv * 27 constants (host) in the boundary launch's
+ * arithmetic (float64 right-hand sides, or for shifted storage the FP32
+ * per-link constants of LBM_BC_FLOAT_FORM); one ghost layer per axis. */
+int lbm_one_time_step_walls(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                            const double* table, const int32_t* sym, void* stream);
+
 /* Step kernel choice of this module: 1 runs periodic steps of 16-bit
  * storage in the staged kernel where the rows allow it (bulk copies of each
  * pulled row into shared memory on the TMA unit, ahead of the compute), 0

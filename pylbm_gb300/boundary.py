@@ -473,3 +473,66 @@ def batch_entries(methods, ext, ghost=None):
             e["iload"] = fwd
         joined = True
     return entries, joined
+
+
+def wall_signature(ghost, shape_in, halo):
+    """Index 9 (o0 + 1) + 3 (o1 + 1) + (o2 + 1) of the walls a ghost slot lies
+    beyond: o_d = -1 below the interior along axis d, +1 above it, else 0."""
+    c = np.asarray(ghost, dtype=np.int64).reshape(len(shape_in), -1)
+    n = np.asarray(shape_in, dtype=np.int64)[:, None]
+    h = np.asarray(halo, dtype=np.int64)[:, None]
+    o = np.where(c < h, -1, np.where(c >= n + h, 1, 0))
+    o = np.concatenate([o, np.zeros((3 - len(shape_in), o.shape[1]), dtype=np.int64)])
+    return 9 * (o[0] + 1) + 3 * (o[1] + 1) + (o[2] + 1)
+
+
+def box_wall_table(methods, shape_in, halo, velocities, constants):
+    """Bounce-back box walls folded into the pull.
+
+    On a box whose every boundary link is a bounce-back link of a wall (no
+    element, no periodic axis, no time-dependent value), the ghost slot
+    (k, x - v_k) a wall node x pulls from holds f_k'(x) + c, k' = opposite
+    of k, written by exactly one link, and c depends only on k and the walls
+    the slot lies beyond.  The step can then read f_k'(x) + c itself instead
+    of the ghost a boundary launch wrote (pylbm/boundary.py:400-469).
+
+    ``constants[m]`` are the per-link constants of method m in the arithmetic
+    of the boundary launch (float64 right-hand sides, or the FP32 constants of
+    the stored deviations).  Returns the table c[k][signature] (27 entries per
+    population, wall_signature) or None when the links do not have that form.
+    """
+    n = np.asarray(shape_in, dtype=np.int64)
+    h = np.asarray(halo, dtype=np.int64)
+    dim = n.size
+    v = np.asarray(velocities, dtype=np.int64).reshape(-1, dim)
+    nv = v.shape[0]
+    if np.any(h != 1) or np.any(np.abs(v) > 1) or not methods:
+        return None
+    if any(m.kind != "bounce_back" or m._timed for m in methods):
+        return None
+    table = np.zeros((nv, 27))
+    seen = np.zeros((nv, 27), dtype=bool)
+    slots = []
+    for m, const in zip(methods, constants):
+        st = np.asarray(m.istore, dtype=np.int64).reshape(-1, dim + 1)
+        il = np.asarray(m.iload[0], dtype=np.int64).reshape(-1, dim + 1)
+        k = st[:, 0]
+        # a bounce-back link loads the opposite population at the fluid node x_g + v_k
+        if np.any(il[:, 1:] != st[:, 1:] + v[k]):
+            return None
+        sig = wall_signature(st[:, 1:].T, n, h)
+        if np.any(sig == 13):  # a store into the interior
+            return None
+        const = np.asarray(const, dtype=np.float64)
+        for kk, ss, cc in zip(k, sig, const):
+            if seen[kk, ss] and table[kk, ss] != cc:
+                return None
+            table[kk, ss] = cc
+            seen[kk, ss] = True
+        slots.append(st[:, 0] * int(np.prod(n + 2 * h)) + np.ravel_multi_index(tuple(st[:, 1:].T), tuple(n + 2 * h)))
+    slots = np.concatenate(slots)
+    # exactly one link for every (population, interior node) whose source leaves the box
+    expected = sum(int(np.prod(n)) - int(np.prod(n - np.abs(vk))) for vk in v)
+    if slots.size != expected or np.unique(slots).size != slots.size:
+        return None
+    return table

@@ -135,6 +135,55 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_step_periodic(const S* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// Bounce-back box walls folded into the pull.  On a box whose boundary links
+// are all bounce-back links of its walls, the ghost slot (k, x - v_k) a wall
+// node x pulls from would hold f_k'(x) + c (k' opposite to k) after the
+// boundary launch, with c given by k and the walls the slot lies beyond
+// (host: boundary.box_wall_table).  The step reads f_k'(x) and adds c itself,
+// in the boundary launch's arithmetic, and rounds the value through the
+// storage type as the ghost store would: the populations equal those of the
+// boundary launch followed by k_step_ghost bit for bit, without the launch
+// and without reading or writing ghost slots.
+struct WallArgs {
+  R c[LBM_Q][27];  // constant by population and wall signature 9 (o0+1) + 3 (o1+1) + (o2+1)
+  int sym[LBM_Q];  // opposite population
+};
+
+__device__ __forceinline__ R through_storage(R v) {
+  S t;
+  Store<S>::store(&t, v);
+  return (R)Store<S>::load(&t);
+}
+
+// wall offset of the source of a node at (lo, hi) faces for a velocity component
+__device__ __forceinline__ int wall_off(int v, bool lo, bool hi) { return (v > 0 && lo) ? -1 : ((v < 0 && hi) ? 1 : 0); }
+
+__global__ void __launch_bounds__(LBM_BLOCK) k_step_walls(const S* __restrict__ f, S* __restrict__ fnew,
+                                                          StepArgs a, WallArgs w) {
+  int i0, i1, i2;
+  if (!my_node(a.g, i0, i1, i2)) return;
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  const bool lo0 = i0 == a.g.h[0], hi0 = i0 == a.g.h[0] + a.g.n[0] - 1;
+  const bool lo1 = LBM_DIM > 1 && i1 == a.g.h[1], hi1 = LBM_DIM > 1 && i1 == a.g.h[1] + a.g.n[1] - 1;
+  const bool lo2 = LBM_DIM > 2 && i2 == a.g.h[2], hi2 = LBM_DIM > 2 && i2 == a.g.h[2] + a.g.n[2] - 1;
+  R g[LBM_Q];
+#define LBM_PULL_WALL(k, vx, vy, vz)                                                                       \
+  {                                                                                                        \
+    const int sig = 9 * (wall_off(vx, lo0, hi0) + 1) + 3 * (wall_off(vy, lo1, hi1) + 1) +                 \
+                    (wall_off(vz, lo2, hi2) + 1);                                                          \
+    if (sig == 13)                                                                                         \
+      g[k] = (R)Store<S>::load(f + o + a.pull[k]);                                                         \
+    else                                                                                                   \
+      g[k] = through_storage((R)Store<S>::load(f + o + (long long)w.sym[k] * a.g.vstride) + w.c[k][sig]); \
+  }
+  LBM_FOR_EACH_V(LBM_PULL_WALL)
+#undef LBM_PULL_WALL
+  lbm_collide<R>(g, a.prm);
+#pragma unroll
+  for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * a.g.vstride, g[k]);
+}
+
+// ---------------------------------------------------------------------------
 // Two nodes per thread (16-bit storage).  A thread owns nodes z and z+1 of the
 // contiguous axis (z even), loads each population of both as one 32-bit word,
 // and runs the generated algebra once on F2 = two FP32 lanes (packed FP32x2
@@ -286,6 +335,67 @@ __global__ void __launch_bounds__(LBM_BLOCK, LBM_PAIRS_MIN_BLOCKS) k_step_ghost_
   gv[k] = pull_pair_ghost(f + o + (long long)(k) * a.g.vstride + LBM_OUTER_GHOST(vx, vy, vz), LBM_VL(vx, vy, vz));
   LBM_FOR_EACH_V(LBM_PULL_GHOST)
 #undef LBM_PULL_GHOST
+  collide_store_pairs(fnew, a.g, prm, i0, i1, i2, gv);
+}
+
+// the box-wall fold for two nodes (z, z + 1) per thread (16-bit storage)
+__global__ void __launch_bounds__(LBM_BLOCK, LBM_PAIRS_MIN_BLOCKS) k_step_walls_pairs(const S* __restrict__ f,
+                                                                                     S* __restrict__ fnew,
+                                                                                     StepArgs a, WallArgs w) {
+  constexpr int L = LBM_DIM - 1;
+  const int z = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int nL = a.g.n[L];
+  if (z >= nL) return;
+  int i0, i1, i2;
+#if LBM_DIM == 1
+  i0 = z + a.g.h[0];
+  i1 = i2 = 0;
+#elif LBM_DIM == 2
+  i0 = blockIdx.y + a.g.h[0];
+  i1 = z + a.g.h[1];
+  i2 = 0;
+#else
+  i0 = blockIdx.z + a.g.h[0];
+  i1 = blockIdx.y + a.g.h[1];
+  i2 = z + a.g.h[2];
+#endif
+  lbm::F2 prm[kPrm];
+#pragma unroll
+  for (int p = 0; p < kPrm; ++p) prm[p] = lbm::F2((float)a.prm[p]);
+  const long long o = lbm::node_offset(a.g, i0, i1, i2);
+  // faces of the outer axes (shared by both nodes) and of the contiguous axis (per node)
+  const bool lo0 = LBM_DIM > 1 && i0 == a.g.h[0], hi0 = LBM_DIM > 1 && i0 == a.g.h[0] + a.g.n[0] - 1;
+  const bool lo1 = LBM_DIM > 2 && i1 == a.g.h[1], hi1 = LBM_DIM > 2 && i1 == a.g.h[1] + a.g.n[1] - 1;
+  const bool first = z == 0, last = z + 2 == nL;
+  lbm::F2 gv[LBM_Q];
+  // wall signature 9 (o0+1) + 3 (o1+1) + (o2+1): the outer axes' part, and the
+  // weight of the contiguous axis
+#if LBM_DIM == 1
+#define LBM_WALL_BASE(vx, vy, vz) 13
+  constexpr int wL = 9;
+#elif LBM_DIM == 2
+#define LBM_WALL_BASE(vx, vy, vz) (9 * (wall_off(vx, lo0, hi0) + 1) + 4)
+  constexpr int wL = 3;
+#else
+#define LBM_WALL_BASE(vx, vy, vz) (9 * (wall_off(vx, lo0, hi0) + 1) + 3 * (wall_off(vy, lo1, hi1) + 1) + 1)
+  constexpr int wL = 1;
+#endif
+#define LBM_PULL_WALL_PAIR(k, vx, vy, vz)                                                             \
+  {                                                                                                   \
+    const int vl = LBM_VL(vx, vy, vz);                                                                \
+    const int base = LBM_WALL_BASE(vx, vy, vz);                                                       \
+    const int s0 = base + wL * wall_off(vl, first, false);                                            \
+    const int s1 = base + wL * wall_off(vl, false, last);                                             \
+    gv[k] = pull_pair_ghost(f + o + (long long)(k) * a.g.vstride + LBM_OUTER_GHOST(vx, vy, vz), vl); \
+    if (s0 != 13 || s1 != 13) {                                                                       \
+      const float2 bb = Pair<S>::load(f + o + (long long)w.sym[k] * a.g.vstride);                     \
+      if (s0 != 13) gv[k].v.x = through_storage(bb.x + w.c[k][s0]);                                 \
+      if (s1 != 13) gv[k].v.y = through_storage(bb.y + w.c[k][s1]);                                 \
+    }                                                                                                 \
+  }
+  LBM_FOR_EACH_V(LBM_PULL_WALL_PAIR)
+#undef LBM_PULL_WALL_PAIR
+#undef LBM_WALL_BASE
   collide_store_pairs(fnew, a.g, prm, i0, i1, i2, gv);
 }
 
@@ -1061,6 +1171,38 @@ int lbm_one_time_step(const void* f, void* fnew, const lbm_lattice* lat, const d
 int lbm_one_time_step_periodic(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
                                void* stream) {
   return step_common(f, fnew, lat, prm, stream, true, "lbm_one_time_step_periodic");
+}
+
+int lbm_one_time_step_walls(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                            const double* table, const int32_t* sym, void* stream) {
+  using namespace lbm_scheme;
+  const char* who = "lbm_one_time_step_walls";
+  int rc = check_pop_lattice(lat, who);
+  if (rc) return rc;
+  if (!f || !fnew || f == fnew) return lbm::fail(LBM_ERR_ARG, "%s: bad population buffers", who);
+  if (!table || !sym) return lbm::fail(LBM_ERR_ARG, "%s: NULL wall table", who);
+  if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "%s: %d parameters expected", who, LBM_NPRM);
+  if (LBM_VMAX != 1) return lbm::fail(LBM_ERR_UNSUPPORTED, "%s: stencils reaching one node only", who);
+  for (int d = 0; d < LBM_DIM; ++d)
+    if (lat->halo[d] != 1) return lbm::fail(LBM_ERR_ARG, "%s: halo[%d]=%d, one ghost layer expected", who, d, lat->halo[d]);
+  WallArgs w;
+  for (int k = 0; k < LBM_Q; ++k) {
+    if (sym[k] < 0 || sym[k] >= LBM_Q) return lbm::fail(LBM_ERR_ARG, "%s: sym[%d]=%d", who, k, sym[k]);
+    w.sym[k] = sym[k];
+    for (int j = 0; j < 27; ++j) w.c[k][j] = (R)table[k * 27 + j];
+  }
+  StepArgs a = make_step_args(*lat, prm);
+  dim3 grid = node_grid(*lat, false);
+  cudaStream_t s = (cudaStream_t)stream;
+#if LBM_HAS_PAIRS
+  if (pairs_fit(*lat, f, fnew)) {
+    grid.x = (unsigned)((lat->n[LBM_DIM - 1] / 2 + LBM_BLOCK - 1) / LBM_BLOCK);
+    k_step_walls_pairs<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a, w);
+    return lbm::launch_check(who);
+  }
+#endif
+  k_step_walls<<<grid, LBM_BLOCK, 0, s>>>((const S*)f, (S*)fnew, a, w);
+  return lbm::launch_check(who);
 }
 
 int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* stream) {

@@ -448,6 +448,7 @@ class SchemeModule:
         _sig(lib, "lbm_scheme_describe", I32, [P, P, P, P, P, P, P])
         _sig(lib, "lbm_one_time_step", I32, [P, P, LP, P, P])
         _sig(lib, "lbm_one_time_step_periodic", I32, [P, P, LP, P, P])
+        _sig(lib, "lbm_one_time_step_walls", I32, [P, P, LP, P, P, P, P])
         _sig(lib, "lbm_transport", I32, [P, P, LP, P])
         _sig(lib, "lbm_f2m", I32, [P, LP, P, LP, P])
         _sig(lib, "lbm_f2m_conserved", I32, [P, LP, P, LP, P])

@@ -29,7 +29,7 @@ import numpy as np
 import sympy as sp
 
 from . import runtime
-from .boundary import Boundary, batch_entries, observed_ghost_copies
+from .boundary import Boundary, batch_entries, box_wall_table, observed_ghost_copies
 from .codegen import SchemeSource
 from .domain import Domain
 from .scheme import Scheme
@@ -225,6 +225,8 @@ class Simulation:
         self._batch_rhs = []        # (device array, method index, host builder) of batch right-hand sides that follow time_bc
         self._full_halo = True
         self.batch_boundary = True  # one launch for all boundary methods where the lists allow it
+        self.fold_walls = True      # bounce-back box walls applied in the pull where the links allow it
+        self._walls = None          # (constants nv x 27, opposite populations) of lbm_one_time_step_walls
         self._graph = None
         self._graph_key = None
         self._need_init = True
@@ -376,6 +378,25 @@ class Simulation:
             self._bc_dev.append((meth, dev))
         self._upload_ghost()
         self._bc_batch = self._batch_table()
+        self._walls = self._wall_table()
+
+    def _wall_table(self):
+        """Constants of the bounce-back box walls folded into the step, or None."""
+        if self.periodic or self._full_halo or self._ghost is not None or self.dim > 3:
+            return None
+        float_form = self.storage != "float64"
+        if not float_form and any(self._lat.shift[k] for k in range(self.scheme.nv)):
+            return None
+        if float_form:
+            consts = [self._float_constants(m.kind, m.iload, m.istore, m.rhs, None) for m in self.bc.methods]
+        else:
+            consts = [np.asarray(m.rhs, dtype=np.float64) for m in self.bc.methods]
+        table = box_wall_table(self.bc.methods, self.domain.shape_in, self.domain.halo,
+                               self.scheme.stencil.get_all_velocities(), consts)
+        if table is None:
+            return None
+        sym = np.ascontiguousarray(self.scheme.stencil.get_symmetric(), dtype=np.int32)
+        return np.ascontiguousarray(table.reshape(-1), dtype=np.float64), sym
 
     def _upload_ghost(self):
         """The ghost copies a step observes (``halo='observed'``), else the full refresh."""
@@ -584,7 +605,7 @@ class Simulation:
 
     def launches_per_step(self):
         """Kernel launches of one step: ghost refresh, boundary methods, step."""
-        if self.periodic:
+        if self.periodic or self._folded():
             return 1
         batch = self._bc_batch is not None and self.batch_boundary
         n = 1
@@ -596,7 +617,19 @@ class Simulation:
             n += 2 if meth.kind == "bouzidi_bounce_back" and dev["ordered"] else 1
         return n
 
+    def _folded(self):
+        return self._walls is not None and self.fold_walls and getattr(self, "closure", None) is None
+
+    def _launch_walls_step(self, F, Fnew, pp):
+        table, sym = self._walls
+        self.module.call(self.module.lib.lbm_one_time_step_walls(
+            F.handle, Fnew.handle, ctypes.byref(self._lat), pp, table.ctypes.data_as(ctypes.c_void_p),
+            sym.ctypes.data_as(ctypes.c_void_p), self._stream))
+
     def _enqueue_step(self, F, Fnew, prm):
+        if self._folded():
+            self._launch_walls_step(F, Fnew, prm.ctypes.data_as(ctypes.c_void_p))
+            return
         if not self.periodic:
             self._enqueue_boundary(F)
         self._launch_step(F, Fnew, prm.ctypes.data_as(ctypes.c_void_p))
@@ -625,10 +658,13 @@ class Simulation:
             self._initialize()
         self._update_m = True
         self._m_cache = {}
-        if not self.periodic:
-            self.boundary_condition()
         prm = self._prm()
-        self._launch_step(self._F, self._Fnew, prm.ctypes.data_as(ctypes.c_void_p))
+        if self._folded():
+            self._launch_walls_step(self._F, self._Fnew, prm.ctypes.data_as(ctypes.c_void_p))
+        else:
+            if not self.periodic:
+                self.boundary_condition()
+            self._launch_step(self._F, self._Fnew, prm.ctypes.data_as(ctypes.c_void_p))
         self._F, self._Fnew = self._Fnew, self._F
         self.t += self.dt
         self.nt += 1
@@ -782,7 +818,7 @@ class Simulation:
             rc = self._core.lbm_graph_end(self._stream, ctypes.byref(g))
         runtime.check(rc)
         self._graph = g
-        self._graph_key = (self._F.ptr, self._Fnew.ptr, tuple(prm))
+        self._graph_key = (self._F.ptr, self._Fnew.ptr, tuple(prm), self._folded(), self.batch_boundary)
 
     def run(self, nsteps, graph=True):
         """Advance ``nsteps`` time steps (same result as calling one_time_step)."""
@@ -795,7 +831,7 @@ class Simulation:
                 self.one_time_step()
             return
         prm = self._prm()
-        if self._graph_key != (self._F.ptr, self._Fnew.ptr, tuple(prm)):
+        if self._graph_key != (self._F.ptr, self._Fnew.ptr, tuple(prm), self._folded(), self.batch_boundary):
             self._capture(prm)
         for _ in range(nsteps // 2):
             runtime.check(self._core.lbm_graph_launch(self._graph, self._stream))

@@ -158,7 +158,8 @@ def runtime_scheme_symbols():
             "lbm_equilibrium", "lbm_relaxation", "lbm_scheme_last_error", "lbm_scheme_describe",
             "lbm_ensemble_step", "lbm_ensemble_step_pairs", "lbm_one_time_step_periodic_closure",
             "lbm_f2m_conserved", "lbm_source_term", "lbm_scheme_set_step_variant", "lbm_scheme_wait_timeouts",
-            "lbm_init_conserved", "lbm_f2m_conserved_dense"}
+            "lbm_init_conserved", "lbm_f2m_conserved_dense",
+            "lbm_one_time_step_walls"}
 
 
 def test_scheme_module_builds_and_exports_header():
