@@ -368,6 +368,18 @@ class PinnedBuffer:
             pass
 
 
+def mapped_device_pointer(array):
+    """Device address of a C-contiguous numpy array in page-locked host memory
+    (``pinned_empty``), or None: kernels can then read or write it directly
+    over the host link instead of a staged copy."""
+    if not isinstance(array, np.ndarray) or not array.flags["C_CONTIGUOUS"] or not isinstance(array, _PinnedArray):
+        return None
+    dev = ctypes.c_void_p()
+    if core().lbm_host_device_pointer(ctypes.c_void_p(array.ctypes.data), ctypes.byref(dev)) != 0:
+        return None
+    return dev
+
+
 def fp64_fma_rate(iters=4096, stream=None):
     """Measured FP64 FMA rate of the current device in flop/s (lbm_fp64_fma_rate)."""
     lib = core()

@@ -657,6 +657,7 @@ class Simulation:
         if self._need_init:
             self._initialize()
         self._update_m = True
+        self._eq_pending = False
         self._m_cache = {}
         prm = self._prm()
         if self._folded():
@@ -782,18 +783,22 @@ class Simulation:
         kernel writes it into the padded layout."""
         if self._need_init:
             self._initialize()
-        if self._eq_pending:  # the other planes as pylbm's equilibrium() left them
+        if self._eq_pending and not self._update_m:  # the other planes as pylbm's equilibrium() left them
             self._moments_for(None)
         first, count, many = self._plane_range(key)
         shape = ((count,) if many else ()) + tuple(self.domain.shape_halo)
-        src = np.asarray(value)
+        src = value if isinstance(value, np.ndarray) else np.asarray(value)
         if src.dtype != np.float64 or src.shape != shape or not src.flags["C_CONTIGUOUS"]:
             src = np.ascontiguousarray(np.broadcast_to(src.astype(np.float64, copy=False), shape))
-        stage = self._stage(src.nbytes)
-        runtime.check(self._core.lbm_memcpy(stage.handle, src.ctypes.data_as(ctypes.c_void_p), src.nbytes,
-                                            runtime.H2D, self._stream))
+        direct = runtime.mapped_device_pointer(src)
+        if direct is None:  # one contiguous copy to the device, then into the layout
+            stage = self._stage(src.nbytes)
+            runtime.check(self._core.lbm_memcpy(stage.handle, src.ctypes.data_as(ctypes.c_void_p), src.nbytes,
+                                                runtime.H2D, self._stream))
+            direct = stage.handle
+        # page-locked arrays are read by the kernel itself over the host link
         runtime.check(self._core.lbm_copy_planes(self._mbuf().handle, ctypes.byref(self._mlat), first, count, 1,
-                                                 stage.handle, 1, self._stream))
+                                                 direct, 1, self._stream))
         self.synchronize()  # ``value`` may be a temporary
         for i in range(first, first + count):
             self._m_cache.pop(i, None)
@@ -839,6 +844,7 @@ class Simulation:
             self.t += self.dt
             self.nt += 2
         self._update_m = True
+        self._eq_pending = False
         self._m_cache = {}
         if nsteps % 2:
             self.one_time_step()
@@ -896,17 +902,19 @@ class Simulation:
             out = np.empty(shape, dtype=np.float64)
         elif out.shape != shape or out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"]:
             raise ValueError(f"fields(out=...) needs a C-contiguous float64 array of shape {shape}")
+        # page-locked arrays are written by the kernel itself over the host link
+        direct = runtime.mapped_device_pointer(out)
+        dst = direct if direct is not None else self._stage(out.nbytes).handle
         if self._update_m:
             # straight from the populations, without the moment array
-            stage = self._stage(out.nbytes)
-            self.module.call(self.module.lib.lbm_f2m_conserved_dense(self._F.handle, ctypes.byref(self._lat),
-                                                                     stage.handle, self._stream))
+            self.module.call(self.module.lib.lbm_f2m_conserved_dense(self._F.handle, ctypes.byref(self._lat), dst,
+                                                                     self._stream))
         else:  # the moment array holds values the user set: read those
-            stage = self._stage(out.nbytes)
             runtime.check(self._core.lbm_copy_planes(self._mbuf().handle, ctypes.byref(self._mlat), 0, nc, 0,
-                                                     stage.handle, 0, self._stream))
-        runtime.check(self._core.lbm_memcpy(out.ctypes.data_as(ctypes.c_void_p), stage.handle, out.nbytes,
-                                            runtime.D2H, self._stream))
+                                                     dst, 0, self._stream))
+        if direct is None:
+            runtime.check(self._core.lbm_memcpy(out.ctypes.data_as(ctypes.c_void_p), dst, out.nbytes,
+                                                runtime.D2H, self._stream))
         self.synchronize()
         names = sorted(self.scheme.consm.items(), key=lambda kv: kv[1])
         return {str(c): out[i] for c, i in names}
