@@ -251,6 +251,7 @@ typedef struct lbm_domain {
 
 #define LBM_ELEMENT_CIRCLE 1        /* p = cx, cy, radius; one label */
 #define LBM_ELEMENT_PARALLELOGRAM 2 /* p = point x, y, v1 x, y, v2 x, y; labels of the 4 edges */
+#define LBM_ELEMENT_SPHERE 3        /* p = cx, cy, cz, radius; one label (3D domains) */
 
 typedef struct lbm_element {
   int32_t kind;

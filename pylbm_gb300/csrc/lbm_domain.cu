@@ -121,7 +121,11 @@ __device__ __forceinline__ void region_node(const Region& r, long long t, int (&
   i[0] = r.lo[0] + (int)(q / n1);
 }
 
-__device__ __forceinline__ bool inside(const lbm_element& e, double x, double y) {
+__device__ __forceinline__ bool inside(const lbm_element& e, double x, double y, double z) {
+  if (e.kind == LBM_ELEMENT_SPHERE) {
+    const double px = sub(x, e.p[0]), py = sub(y, e.p[1]), pz = sub(z, e.p[2]);
+    return add(add(mul(px, px), mul(py, py)), mul(pz, pz)) <= mul(e.p[3], e.p[3]);
+  }
   if (e.kind == LBM_ELEMENT_CIRCLE) {
     const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
     return add(mul(px, px), mul(py, py)) <= mul(e.p[2], e.p[2]);
@@ -136,6 +140,66 @@ __device__ __forceinline__ bool inside(const lbm_element& e, double x, double y)
 
 // first crossing of the ray (x, y) + t v, t in (0, dmax], with the element
 // boundary: t (or -1) and the label of the crossed edge (or -1)
+// the ray (x, y, z) + t v against the sphere, as the host evaluates the
+// ellipsoid quadratic with the semi-axes r e_x, r e_y, r e_z (cross products,
+// then the quadratic's coefficients, term by term in the host's order)
+__device__ __forceinline__ double sphere_crossing(const lbm_element& e, double x, double y, double z, double v0,
+                                                 double v1, double v2, double dmax, int& border) {
+  const double r = e.p[3];
+  const double a[3] = {mul(r, 1.0), mul(r, 0.0), mul(r, 0.0)};
+  const double b[3] = {mul(r, 0.0), mul(r, 1.0), mul(r, 0.0)};
+  const double c[3] = {mul(r, 0.0), mul(r, 0.0), mul(r, 1.0)};
+  auto cross = [](const double (&u)[3], const double (&w)[3], double (&out)[3]) {
+    out[0] = sub(mul(u[1], w[2]), mul(u[2], w[1]));
+    out[1] = sub(mul(u[2], w[0]), mul(u[0], w[2]));
+    out[2] = sub(mul(u[0], w[1]), mul(u[1], w[0]));
+  };
+  double c12[3], c23[3], c31[3];
+  cross(a, b, c12);
+  cross(b, c, c23);
+  cross(c, a, c31);
+  const double in = add(add(mul(a[0], c23[0]), mul(a[1], c23[1])), mul(a[2], c23[2]));
+  const double dd = mul(in, in);
+  const double cxx = add(add(mul(c12[0], c12[0]), mul(c23[0], c23[0])), mul(c31[0], c31[0]));
+  const double cyy = add(add(mul(c12[1], c12[1]), mul(c23[1], c23[1])), mul(c31[1], c31[1]));
+  const double czz = add(add(mul(c12[2], c12[2]), mul(c23[2], c23[2])), mul(c31[2], c31[2]));
+  const double cxy = mul(2.0, add(add(mul(c12[0], c12[1]), mul(c23[0], c23[1])), mul(c31[0], c31[1])));
+  const double cyz = mul(2.0, add(add(mul(c12[1], c12[2]), mul(c23[1], c23[2])), mul(c31[1], c31[2])));
+  const double czx = mul(2.0, add(add(mul(c12[2], c12[0]), mul(c23[2], c23[0])), mul(c31[2], c31[0])));
+  const double X = sub(x, e.p[0]), Y = sub(y, e.p[1]), Z = sub(z, e.p[2]);
+  const double qa = add(add(add(add(add(mul(cxx, mul(v0, v0)), mul(cyy, mul(v1, v1))), mul(czz, mul(v2, v2))),
+                                mul(mul(cxy, v0), v1)),
+                            mul(mul(cyz, v1), v2)),
+                        mul(mul(czx, v2), v0));
+  const double bx = add(add(mul(mul(2.0, cxx), v0), mul(cxy, v1)), mul(czx, v2));
+  const double by = add(add(mul(mul(2.0, cyy), v1), mul(cyz, v2)), mul(cxy, v0));
+  const double bz = add(add(mul(mul(2.0, czz), v2), mul(czx, v0)), mul(cyz, v1));
+  const double qb = add(add(mul(bx, X), mul(by, Y)), mul(bz, Z));
+  const double qc =
+      sub(add(add(add(add(add(mul(cxx, mul(X, X)), mul(cyy, mul(Y, Y))), mul(czz, mul(Z, Z))), mul(mul(cxy, X), Y)),
+                  mul(mul(cyz, Y), Z)),
+              mul(mul(czx, Z), X)),
+          dd);
+  double disc = sub(mul(qb, qb), mul(mul(4.0, qa), qc));
+  const bool ok = disc >= 0;
+  double t1 = kFar, t2 = kFar;
+  if (ok) {
+    disc = __dsqrt_rn(disc);
+    t1 = dvd(sub(-qb, disc), mul(2.0, qa));
+    t2 = dvd(add(-qb, disc), mul(2.0, qa));
+  }
+  if (t1 < 0) t1 = kFar;
+  if (t2 < 0) t2 = kFar;
+  double t = ok ? fmin(t1, t2) : -1.0;
+  if (t == kFar) t = -1.0;
+  border = -1;
+  if (t > 0 && t <= dmax) {
+    border = e.label[0];
+    return t;
+  }
+  return -1.0;
+}
+
 __device__ __forceinline__ double crossing(const lbm_element& e, double x, double y, double vx, double vy,
                                           double dmax, int& border) {
   border = -1;
@@ -200,18 +264,18 @@ __device__ __forceinline__ long long box_offset(const Box& b, const int (&i)[3])
 }
 
 __global__ void k_element_map(Box b, Region r, lbm_element e, const double* __restrict__ c0,
-                              const double* __restrict__ c1, double* ioo) {
+                              const double* __restrict__ c1, const double* __restrict__ c2, double* ioo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= r.nodes) return;
   int i[3];
   region_node(r, t, i);
-  const bool in = inside(e, c0[i[0]], c1[i[1]]);
+  const bool in = inside(e, c0[i[0]], c1[i[1]], c2 ? c2[i[2]] : 0.0);
   if (in) ioo[box_offset(b, i)] = e.isfluid ? kValIn : kValOut;
 }
 
 __global__ void k_element_links(Box b, lbm_domain d, Region r, lbm_element e, const double* __restrict__ c0,
-                                const double* __restrict__ c1, const double* __restrict__ ioo, double* dist,
-                                int* flag) {
+                                const double* __restrict__ c1, const double* __restrict__ c2,
+                                const double* __restrict__ ioo, double* dist, int* flag) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= r.nodes * b.nu) return;
   const int u = (int)(t / r.nodes);
@@ -219,14 +283,18 @@ __global__ void k_element_links(Box b, lbm_domain d, Region r, lbm_element e, co
   if (vx == 0 && vy == 0 && vz == 0) return;
   int i[3];
   region_node(r, t - (long long)u * r.nodes, i);
-  const double x = c0[i[0]], y = c1[i[1]];
-  const bool in = inside(e, x, y);
+  const double x = c0[i[0]], y = c1[i[1]], z = c2 ? c2[i[2]] : 0.0;
+  const bool in = inside(e, x, y, z);
   const bool solid = e.isfluid ? !in : in;
   const long long o = box_offset(b, i);
   int j[3] = {i[0] + vx, i[1] + vy, i[2] + vz};
   const bool out = ioo[box_offset(b, j)] == kValOut;
   int border;
-  const double alpha = crossing(e, x, y, mul(d.dx, (double)vx), mul(d.dx, (double)vy), 1.0, border);
+  const double alpha =
+      e.kind == LBM_ELEMENT_SPHERE
+          ? sphere_crossing(e, x, y, z, mul(d.dx, (double)vx), mul(d.dx, (double)vy), mul(d.dx, (double)vz), 1.0,
+                            border)
+          : crossing(e, x, y, mul(d.dx, (double)vx), mul(d.dx, (double)vy), 1.0, border);
   const bool sel = alpha > 0 && !solid && out;
   double dk = dist[(long long)u * b.nodes + o];
   int fk = flag[(long long)u * b.nodes + o];
@@ -340,9 +408,10 @@ int lbm_domain_element(const lbm_domain* d, const lbm_element* e, const double* 
   int rc = check_domain(d, "lbm_domain_element");
   if (rc) return rc;
   if (!e || !coords || !in_or_out || !distance || !flag) return fail(LBM_ERR_ARG, "lbm_domain_element: NULL argument");
-  if (d->dim != 2) return fail(LBM_ERR_UNSUPPORTED, "lbm_domain_element: 2D elements only (dim=%d)", d->dim);
-  if (e->kind != LBM_ELEMENT_CIRCLE && e->kind != LBM_ELEMENT_PARALLELOGRAM)
+  if (e->kind != LBM_ELEMENT_CIRCLE && e->kind != LBM_ELEMENT_PARALLELOGRAM && e->kind != LBM_ELEMENT_SPHERE)
     return fail(LBM_ERR_ARG, "lbm_domain_element: kind %d", e->kind);
+  if (d->dim != (e->kind == LBM_ELEMENT_SPHERE ? 3 : 2))
+    return fail(LBM_ERR_UNSUPPORTED, "lbm_domain_element: element kind %d on a %dD domain", e->kind, d->dim);
   Region r;
   r.nodes = 1;
   for (int a = 0; a < 3; ++a) {
@@ -359,10 +428,12 @@ int lbm_domain_element(const lbm_domain* d, const lbm_element* e, const double* 
   cudaStream_t s = (cudaStream_t)stream;
   const double* c0 = coords;
   const double* c1 = coords + d->n[0];
-  k_element_map<<<blocks_for(r.nodes), kThreads, 0, s>>>(b, r, *e, c0, c1, in_or_out);
+  const double* c2 = d->dim == 3 ? coords + d->n[0] + d->n[1] : nullptr;
+  k_element_map<<<blocks_for(r.nodes), kThreads, 0, s>>>(b, r, *e, c0, c1, c2, in_or_out);
   rc = launch_check("lbm_domain_element");
   if (rc) return rc;
-  k_element_links<<<blocks_for(r.nodes * b.nu), kThreads, 0, s>>>(b, *d, r, *e, c0, c1, in_or_out, distance, flag);
+  k_element_links<<<blocks_for(r.nodes * b.nu), kThreads, 0, s>>>(b, *d, r, *e, c0, c1, c2, in_or_out, distance,
+                                                                  flag);
   return launch_check("lbm_domain_element");
 }
 

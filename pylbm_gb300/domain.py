@@ -226,6 +226,9 @@ class Domain:
         elif isinstance(elem, geometry.Parallelogram):
             e.kind = runtime.LBM_ELEMENT_PARALLELOGRAM
             vals = [*elem.point, *elem.v1, *elem.v2]
+        elif isinstance(elem, geometry.Sphere):
+            e.kind = runtime.LBM_ELEMENT_SPHERE
+            vals = [*elem.center, elem.radius]
         else:
             raise NotImplementedError(f"{type(elem).__name__} is not built on the device")
         for i, v in enumerate(vals):

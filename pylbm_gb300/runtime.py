@@ -60,6 +60,7 @@ LBM_MAX_PRM = 8
 LBM_INSTANCE_PAIRS = 1
 LBM_ELEMENT_CIRCLE = 1
 LBM_ELEMENT_PARALLELOGRAM = 2
+LBM_ELEMENT_SPHERE = 3
 
 
 class DomainDesc(ctypes.Structure):

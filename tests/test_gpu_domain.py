@@ -24,7 +24,19 @@ CASES = {
     "poiseuille_3d": lambda: demo_cases.poiseuille_3d(),
     "euler_1d": lambda: demo_cases.euler_1d(),
     "rayleigh_benard": lambda: demo_cases.rayleigh_benard(),
+    # 3D: pylbm's flow past a sphere (D3Q15, Bouzidi on the sphere) and a
+    # sphere in the lid-driven cube (D3Q19, off-grid centre)
+    "karman_3d": lambda: demo_cases.karman_3d(),
+    "sphere_cube": lambda: _sphere_cube(),
 }
+
+
+def _sphere_cube():
+    from pylbm_gb300.geometry import Sphere
+    d = W.cavity3d(n=40)
+    d["elements"] = [Sphere((0.43, 0.51, 0.37), 0.17, label=2)]
+    d["boundary_conditions"][2] = {"method": {0: d["boundary_conditions"][0]["method"][0]}}
+    return d
 
 
 @pytest.mark.parametrize("name", list(CASES))
