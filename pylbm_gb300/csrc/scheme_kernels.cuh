@@ -149,11 +149,18 @@ struct WallArgs {
   int sym[LBM_Q];  // opposite population
 };
 
-__device__ __forceinline__ R through_storage(R v) {
-  S t;
-  Store<S>::store(&t, v);
-  return (R)Store<S>::load(&t);
-}
+// v rounded to the storage type and back, in registers: what a store to the
+// ghost slot and the step's load of it would give
+template <typename T> struct StorageRound {
+  __device__ __forceinline__ static R apply(R v) { return v; }  // float / double: exact
+};
+template <> struct StorageRound<__half> {
+  __device__ __forceinline__ static R apply(R v) { return (R)__half2float(__float2half_rn((float)v)); }
+};
+template <> struct StorageRound<__nv_bfloat16> {
+  __device__ __forceinline__ static R apply(R v) { return (R)__bfloat162float(__float2bfloat16_rn((float)v)); }
+};
+__device__ __forceinline__ R through_storage(R v) { return StorageRound<S>::apply(v); }
 
 // wall offset of the source of a node at (lo, hi) faces for a velocity component
 __device__ __forceinline__ int wall_off(int v, bool lo, bool hi) { return (v > 0 && lo) ? -1 : ((v < 0 && hi) ? 1 : 0); }

@@ -384,6 +384,8 @@ class Simulation:
         """Constants of the bounce-back box walls folded into the step, or None."""
         if self.periodic or self._full_halo or self._ghost is not None or self.dim > 3:
             return None
+        if any(m.kind != "bounce_back" for m in self.bc.methods):
+            return None
         float_form = self.storage != "float64"
         if not float_form and any(self._lat.shift[k] for k in range(self.scheme.nv)):
             return None
