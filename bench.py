@@ -195,9 +195,9 @@ def variants(args):
 # FP64-pipe instructions (DADD + DMUL + DFMA) per node of the FP64 step
 # kernels, from an ncu capture of the same kernels (a property of the compiled
 # code; profiles/ncu_fp64_step_counts.md): the exact-constant D3Q19 form uses
-# 131 DADD + 14 DMUL + 84 DFMA, the printed (parity) D2Q9 form, compiled
-# without contraction, 114 DADD + 33 DMUL
-FP64_INST_PER_NODE = {"tgv3d_256_f64": 229, "cavity_256_f64_parity": 147}
+# 131 DADD + 14 DMUL + 84 DFMA, the printed (parity) D2Q9 form of the cavity,
+# compiled without contraction and with its walls in the step, 110 DADD + 33 DMUL
+FP64_INST_PER_NODE = {"tgv3d_256_f64": 229, "cavity_256_f64_parity": 143}
 
 
 def fp64_roof(inst_per_node, nodes_per_s):

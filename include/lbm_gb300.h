@@ -373,6 +373,14 @@ int lbm_mlp_sizes(int32_t* nparam, int32_t* nweights_bf16);
 int lbm_mlp_scratch_bytes(int32_t n, size_t* bytes);
 int lbm_mlp_sync_weights(const float* params, void* wbf16, void* stream);
 int lbm_mlp_forward(const void* x, int32_t n, const void* wbf16, const float* params, float* y, void* stream);
+/* The same forward pass on the 5th-generation tensor cores: tiles of 128
+ * samples, tcgen05.mma with the FP32 accumulators in tensor memory, BF16
+ * weights from the FP32 master block params (rounded as
+ * lbm_mlp_sync_weights rounds them); any n >= 0.  Outputs equal those of
+ * lbm_mlp_forward up to the FP32 accumulation order inside a layer.
+ * lbm_mlp_tc_timeouts reads the count of its bounded waits that gave up. */
+int lbm_mlp_forward_tc(const void* x, int32_t n, const float* params, float* y, void* stream);
+int lbm_mlp_tc_timeouts(uint32_t* count);
 /* Adds dLoss/dparams to grad (FP32 atomics; zero it first) for the loss
  * mean over samples and the 6 used outputs of (y - target)^2; writes the
  * loss to *loss (device).  scratch: lbm_mlp_scratch_bytes(n) bytes. */

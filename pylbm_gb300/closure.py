@@ -100,6 +100,21 @@ class Mlp:
         dy.download(y, stream=self.stream)
         return y[:n].astype(np.float64)
 
+    def forward_tc(self, x):
+        """The same outputs from the tcgen05 kernel (lbm_mlp_forward_tc: tiles of
+        128 samples, accumulators in tensor memory), any number of rows."""
+        xb = _bf16_bits(x)
+        n = xb.shape[0]
+        dx = runtime.DeviceBuffer(max(xb.nbytes, 32))
+        dx.upload(xb, stream=self.stream)
+        dy = runtime.DeviceBuffer(max(4 * OUT * n, 4))
+        runtime.check(self._core.lbm_mlp_forward_tc(dx.handle, n, self.p.handle, dy.handle, self.stream))
+        y = np.empty((n, OUT), dtype=np.float32)
+        dy.download(y, stream=self.stream)
+        dx.free()
+        dy.free()
+        return y.astype(np.float64)
+
     def _device_data(self, x, t):
         xb = _bf16_bits(x)
         n = xb.shape[0]

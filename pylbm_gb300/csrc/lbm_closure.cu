@@ -13,6 +13,7 @@
 //                   both layouts the GEMMs use
 #include "lbm_common.cuh"
 #include "lbm_mlp.cuh"
+#include "lbm_mlp_tc.cuh"
 
 using namespace lbm;
 using namespace lbm_mlp;
@@ -399,6 +400,28 @@ int lbm_mlp_forward(const void* x, int32_t n, const void* wbf16, const float* pa
   k_mlp_infer<<<grid_for(n / 16), 32 * kWarps, 0, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)x, n, (const __nv_bfloat16*)wbf16, params, y);
   return launch_check("lbm_mlp_forward");
+}
+
+int lbm_mlp_forward_tc(const void* x, int32_t n, const float* params, float* y, void* stream) {
+  if (!x || !params || !y) return fail(LBM_ERR_ARG, "lbm_mlp_forward_tc: NULL");
+  if (n < 0) return fail(LBM_ERR_ARG, "lbm_mlp_forward_tc: n=%d", n);
+  if (n == 0) return LBM_OK;
+  int dev = 0, sms = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "lbm_mlp_forward_tc: cudaGetDevice");
+  if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "lbm_mlp_forward_tc");
+  if (rc) return rc;
+  const int tiles = (n + lbm_mlp_tc::kRows - 1) / lbm_mlp_tc::kRows;
+  // four blocks per SM hold 4 x 128 of the 512 tensor-memory columns
+  const int blocks = tiles < 4 * sms ? tiles : 4 * sms;
+  lbm_mlp_tc::k_mlp_forward_tc<<<blocks, lbm_mlp_tc::kThreads, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)x, n, params, y);
+  return launch_check("lbm_mlp_forward_tc");
+}
+
+int lbm_mlp_tc_timeouts(uint32_t* count) {
+  if (!count) return fail(LBM_ERR_ARG, "lbm_mlp_tc_timeouts: NULL");
+  return cuda_check(cudaMemcpyFromSymbol(count, lbm_mlp_tc::mlp_tc_timeouts, sizeof(uint32_t)),
+                    "lbm_mlp_tc_timeouts");
 }
 
 int lbm_mlp_gradients(const void* x, const float* target, int32_t n, const void* wbf16, const float* params,

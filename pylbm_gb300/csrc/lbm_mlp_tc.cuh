@@ -1,0 +1,243 @@
+// Batch forward pass of the closure MLP on the 5th-generation tensor cores
+// (tcgen05.mma, accumulators in tensor memory).
+//
+// A block of four warps evaluates 128 samples per tile, one sample per
+// thread row: the BF16 inputs and weights sit in shared memory in the
+// canonical K-major layout without swizzle (8 x 16-byte core matrices), one
+// elected thread issues the layer's MMAs (M = 128, K = 16 per instruction,
+// N = 64 / 64 / 16), their completion arrives on an mbarrier, and each warp
+// reads its 32 rows of the FP32 accumulator with tcgen05.ld, adds the bias,
+// applies SiLU, rounds to BF16 and writes the next layer's operand.  The
+// arithmetic per element is that of the warp-level path (lbm_mlp.cuh); only
+// the order of the FP32 accumulation inside a layer may differ.
+//
+// Tensor memory: 128 columns per block (layer 1 and 3 accumulators share
+// columns 0..63, layer 2 uses 64..127), allocated by warp 0 at the start and
+// freed at the end.  Every mbarrier wait is bounded in time; a block whose
+// wait gives up leaves after all its threads agree (no partial barrier) and
+// counts the timeout.
+#pragma once
+
+#include "lbm_common.cuh"
+#include "lbm_mlp.cuh"
+
+namespace lbm_mlp_tc {
+
+using namespace lbm_mlp;
+
+constexpr int kRows = 128;         // samples per tile (MMA M)
+constexpr int kThreads = 128;      // one thread per sample row
+constexpr uint32_t kTmemCols = 128;
+constexpr int kN3 = 16;            // layer-3 outputs padded to the MMA's smallest N for M = 128
+
+// byte offset of element (r, k) of an [R][K] BF16 operand in the K-major
+// no-swizzle layout: core matrices of 8 rows x 8 elements (128 bytes, rows
+// 16 bytes apart), K-adjacent core matrices 128 bytes apart, row groups of 8
+// (K / 8) * 128 bytes apart
+__device__ __forceinline__ uint32_t core_offset(int r, int k, int K) {
+  return (uint32_t)((((r >> 3) * (K >> 3) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+}
+
+// shared-memory matrix descriptor: start address, leading byte offset (the
+// K-direction core-matrix step), stride byte offset (the 8-row step),
+// descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M
+__host__ __device__ constexpr uint32_t instr_desc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   lbm::smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive accumulator columns of this thread's row (its warp's lanes)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// waits that gave up (0 in a healthy run), read by lbm_mlp_tc_timeouts
+__device__ unsigned int mlp_tc_timeouts;
+
+struct Smem {
+  __nv_bfloat16 w1[H * IN];   // [64][16]  layer-1 B operand (out x in)
+  __nv_bfloat16 w2[H * H];    // [64][64]
+  __nv_bfloat16 w3[kN3 * H];  // [16][64]  (rows 8..15 zero)
+  __nv_bfloat16 x[kRows * IN];
+  __nv_bfloat16 h[kRows * H];  // hidden activations of layer 1, then of layer 2
+  float b1[H], b2[H], b3[OUT];
+  uint64_t bar;
+  uint32_t tmem_base;
+};
+
+__device__ __forceinline__ void store_bf16(unsigned char* base, uint32_t off, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
+}
+
+// wait for the block's MMA commit of the current phase; false when any thread
+// of the block gave up (every thread returns the same answer)
+__device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& phase) {
+  const bool ok = lbm::mbar_wait(bar, phase & 1);
+  ++phase;
+  return __syncthreads_and(ok) != 0;
+}
+
+__global__ void __launch_bounds__(kThreads) k_mlp_forward_tc(const __nv_bfloat16* __restrict__ x, int n,
+                                                             const float* __restrict__ params, float* __restrict__ y) {
+  __shared__ __align__(128) Smem sm;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char* w1b = reinterpret_cast<unsigned char*>(sm.w1);
+  unsigned char* w2b = reinterpret_cast<unsigned char*>(sm.w2);
+  unsigned char* w3b = reinterpret_cast<unsigned char*>(sm.w3);
+  unsigned char* xb = reinterpret_cast<unsigned char*>(sm.x);
+  unsigned char* hb = reinterpret_cast<unsigned char*>(sm.h);
+  // weights: the BF16 rounding of the FP32 master block (as lbm_mlp_sync_weights)
+  for (int i = tid; i < H * IN; i += kThreads) store_bf16(w1b, core_offset(i / IN, i % IN, IN), params[PW1 + i]);
+  for (int i = tid; i < H * H; i += kThreads) store_bf16(w2b, core_offset(i / H, i % H, H), params[PW2 + i]);
+  for (int i = tid; i < kN3 * H; i += kThreads) {
+    const int r = i / H, k = i % H;
+    store_bf16(w3b, core_offset(r, k, H), r < OUT ? params[PW3 + r * H + k] : 0.0f);
+  }
+  for (int i = tid; i < H; i += kThreads) {
+    sm.b1[i] = params[PB1 + i];
+    sm.b2[i] = params[PB2 + i];
+  }
+  for (int i = tid; i < OUT; i += kThreads) sm.b3[i] = params[PB3 + i];
+  if (tid == 0) {
+    lbm::mbar_init(&sm.bar, 1);
+    lbm::mbar_init_fence();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     lbm::smem_addr(&sm.tmem_base)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = sm.tmem_base;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;  // this warp's 32 accumulator rows
+  const uint32_t xa = lbm::smem_addr(sm.x), ha = lbm::smem_addr(sm.h);
+  const uint32_t w1a = lbm::smem_addr(sm.w1), w2a = lbm::smem_addr(sm.w2), w3a = lbm::smem_addr(sm.w3);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int tiles = (n + kRows - 1) / kRows;
+  for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const int row = tile * kRows + tid;
+    // inputs of this thread's sample (zero past the end)
+    {
+      uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
+      if (row < n) {
+        lo = *reinterpret_cast<const uint4*>(x + (size_t)row * IN);
+        hi = *reinterpret_cast<const uint4*>(x + (size_t)row * IN + 8);
+      }
+      *reinterpret_cast<uint4*>(xb + core_offset(tid, 0, IN)) = lo;
+      *reinterpret_cast<uint4*>(xb + core_offset(tid, 8, IN)) = hi;
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    // layer 1: D[0:64) = X (128 x 16) W1^T
+    if (tid == 0) {
+      fence_after_sync();
+      mma_bf16(tmem, smem_desc(xa, 128, (IN / 8) * 128), smem_desc(w1a, 128, (IN / 8) * 128), instr_desc(kRows, H),
+               0);
+      mma_commit(&sm.bar);
+    }
+    if (!(ok = wait_mma(&sm.bar, phase))) break;
+    fence_after_sync();
+#pragma unroll
+    for (int c = 0; c < H; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + lane_base + (uint32_t)c, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, c + j, H), lbm_mlp::silu(v[j] + sm.b1[c + j]));
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    // layer 2: D[64:128) = H1 (128 x 64) W2^T, four K = 16 steps
+    if (tid == 0) {
+      fence_after_sync();
+#pragma unroll
+      for (int kc = 0; kc < H / 16; ++kc)
+        mma_bf16(tmem + 64, smem_desc(ha + kc * 256, 128, (H / 8) * 128), smem_desc(w2a + kc * 256, 128, (H / 8) * 128),
+                 instr_desc(kRows, H), kc > 0);
+      mma_commit(&sm.bar);
+    }
+    if (!(ok = wait_mma(&sm.bar, phase))) break;
+    fence_after_sync();
+#pragma unroll
+    for (int c = 0; c < H; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + lane_base + 64u + (uint32_t)c, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, c + j, H), lbm_mlp::silu(v[j] + sm.b2[c + j]));
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    // layer 3: D[0:16) = H2 (128 x 64) W3^T (outputs 8..15 are zero rows of W3)
+    if (tid == 0) {
+      fence_after_sync();
+#pragma unroll
+      for (int kc = 0; kc < H / 16; ++kc)
+        mma_bf16(tmem, smem_desc(ha + kc * 256, 128, (H / 8) * 128), smem_desc(w3a + kc * 256, 128, (H / 8) * 128),
+                 instr_desc(kRows, kN3), kc > 0);
+      mma_commit(&sm.bar);
+    }
+    if (!(ok = wait_mma(&sm.bar, phase))) break;
+    fence_after_sync();
+    {
+      float v[16];
+      tmem_ld16(tmem + lane_base, v);
+      if (row < n) {
+#pragma unroll
+        for (int j = 0; j < OUT; ++j) y[(size_t)row * OUT + j] = v[j] + sm.b3[j];
+      }
+    }
+    fence_before_sync();
+    __syncthreads();
+  }
+  if (!ok && tid == 0) atomicAdd(&mlp_tc_timeouts, 1u);
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+}  // namespace lbm_mlp_tc

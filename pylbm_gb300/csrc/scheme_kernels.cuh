@@ -174,6 +174,11 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_step_walls(const S* __restrict__ 
   const bool lo1 = LBM_DIM > 1 && i1 == a.g.h[1], hi1 = LBM_DIM > 1 && i1 == a.g.h[1] + a.g.n[1] - 1;
   const bool lo2 = LBM_DIM > 2 && i2 == a.g.h[2], hi2 = LBM_DIM > 2 && i2 == a.g.h[2] + a.g.n[2] - 1;
   R g[LBM_Q];
+  if (!(lo0 || hi0 || lo1 || hi1 || lo2 || hi2)) {
+    // away from the walls (all but the outer layer): the plain pull
+#pragma unroll
+    for (int k = 0; k < LBM_Q; ++k) g[k] = (R)Store<S>::load(f + o + a.pull[k]);
+  } else {
 #define LBM_PULL_WALL(k, vx, vy, vz)                                                                       \
   {                                                                                                        \
     const int sig = 9 * (wall_off(vx, lo0, hi0) + 1) + 3 * (wall_off(vy, lo1, hi1) + 1) +                 \
@@ -183,8 +188,9 @@ __global__ void __launch_bounds__(LBM_BLOCK) k_step_walls(const S* __restrict__ 
     else                                                                                                   \
       g[k] = through_storage((R)Store<S>::load(f + o + (long long)w.sym[k] * a.g.vstride) + w.c[k][sig]); \
   }
-  LBM_FOR_EACH_V(LBM_PULL_WALL)
+    LBM_FOR_EACH_V(LBM_PULL_WALL)
 #undef LBM_PULL_WALL
+  }
   lbm_collide<R>(g, a.prm);
 #pragma unroll
   for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * a.g.vstride, g[k]);
@@ -400,7 +406,15 @@ __global__ void __launch_bounds__(LBM_BLOCK, LBM_PAIRS_MIN_BLOCKS) k_step_walls_
       if (s1 != 13) gv[k].v.y = through_storage(bb.y + w.c[k][s1]);                                 \
     }                                                                                                 \
   }
-  LBM_FOR_EACH_V(LBM_PULL_WALL_PAIR)
+  if (!(lo0 || hi0 || lo1 || hi1 || first || last)) {
+    // away from the walls: the plain two-node pull of the ghost kernel
+#define LBM_PULL_GHOST_W(k, vx, vy, vz) \
+  gv[k] = pull_pair_ghost(f + o + (long long)(k) * a.g.vstride + LBM_OUTER_GHOST(vx, vy, vz), LBM_VL(vx, vy, vz));
+    LBM_FOR_EACH_V(LBM_PULL_GHOST_W)
+#undef LBM_PULL_GHOST_W
+  } else {
+    LBM_FOR_EACH_V(LBM_PULL_WALL_PAIR)
+  }
 #undef LBM_PULL_WALL_PAIR
 #undef LBM_WALL_BASE
   collide_store_pairs(fnew, a.g, prm, i0, i1, i2, gv);
