@@ -342,9 +342,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256, help="grid size per axis")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "karman", "cavity3d", "cavity"],
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "karman", "cavity3d", "cavity", "closure"],
                     help="tgv: the headline D3Q19 workload; cylinder / karman / cavity3d / cavity (D2Q9 n^2): "
-                         "the bounded flows")
+                         "the bounded flows; closure: the Re 30 000 shear layer n^2 with the learned closure")
+    ap.add_argument("--closure-kernel", default="tc", choices=["tc", "warp"],
+                    help="closure workload: tcgen05 MMAs (tc) or warp-level mma.sync (warp)")
     ap.add_argument("--step-variant", type=int, default=0, choices=[0, 1],
                     help="16-bit periodic steps: 1 staged kernel where rows fit, 0 direct-load kernel")
     ap.add_argument("--fp64-form", default="parity", choices=["parity", "exact"],
@@ -389,6 +391,13 @@ def main():
     elif args.workload == "karman":
         sim = Simulation(W.karman(dx=1.0 / 1024), dtype=args.dtype)
         desc = "D2Q9 Geier relative-velocity flow past a disc 2048x1024 (Bouzidi walls and disc, NeumannX)"
+    elif args.workload == "closure":
+        from pylbm_gb300.closure import ClosureModel, study_dicos
+        from pylbm_gb300.closure_study import DEFAULT_MODEL
+        sim = Simulation(study_dicos(100000, n), dtype=args.dtype)
+        sim.set_closure(ClosureModel.load(DEFAULT_MODEL))
+        sim.closure_kernel = args.closure_kernel
+        desc = f"D2Q9 MRT double shear layer {n}^2, Re 30 000, learned closure ({args.closure_kernel} kernel)"
     elif args.workload == "cavity":
         sim = Simulation(W.cavity(n=n), dtype=args.dtype, parity=parity)
         desc = f"D2Q9 MRT lid-driven cavity {n}^2 (bounce-back walls, moving lid)"
@@ -401,7 +410,10 @@ def main():
     buf_bytes = sim._lat.elements * BYTES_PER_VALUE[args.dtype]
     # kernels per step: the step, plus the ghost refresh and the boundary launches
     launches_per_step = sim.launches_per_step()
-    step_kernel = ("lbm_scheme::k_step_periodic_pairs" if sim.periodic and args.dtype in ("float16", "bfloat16")
+    step_kernel = ("lbm_scheme::k_step_periodic_closure" + ("_tc" if args.closure_kernel == "tc" else "")
+                   if args.workload == "closure"
+                   else "lbm_scheme::k_step_walls" if sim._folded()
+                   else "lbm_scheme::k_step_periodic_pairs" if sim.periodic and args.dtype in ("float16", "bfloat16")
                    else "lbm_scheme::k_step_periodic" if sim.periodic else "lbm_scheme::k_step_ghost")
     for _ in range(args.warmup):
         sim.one_time_step()

@@ -455,6 +455,15 @@ int lbm_scheme_wait_timeouts(uint32_t* count);
 int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
                                        const void* wbf16, const float* params, const float* norm,
                                        const float* guard, int32_t* fallbacks, int32_t grid, void* stream);
+/* The same step with the MLP on the 5th-generation tensor cores: 128 nodes
+ * per block tile, one node per thread, the three layers as tcgen05 MMAs with
+ * FP32 accumulators in tensor memory; BF16 weights from the FP32 master block
+ * params (no BF16 copy needed).  Same guard and fallback count; the
+ * corrections equal those of the warp-level kernel up to the FP32
+ * accumulation order inside a layer. */
+int lbm_one_time_step_periodic_closure_tc(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                                          const float* params, const float* norm, const float* guard,
+                                          int32_t* fallbacks, void* stream);
 
 /* Pure pull streaming on the interior (pylbm/algorithm/base.py:289-296). */
 int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* stream);

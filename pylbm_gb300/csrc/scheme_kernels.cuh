@@ -18,6 +18,7 @@
 
 #include "lbm_common.cuh"
 #include "lbm_mlp.cuh"
+#include "lbm_tc.cuh"
 
 #include <type_traits>
 
@@ -29,6 +30,9 @@ namespace lbm_scheme {
 
 using lbm::Geo;
 using lbm::Store;
+
+// bounded waits of this module's kernels that gave up (0 in a healthy run)
+__device__ unsigned int lbm_wait_timeouts;
 using S = LBM_STORAGE;
 using R = LBM_COMPUTE;
 
@@ -467,8 +471,6 @@ constexpr int kStages = 4;
 constexpr int kConsumers = 4;  // warps
 constexpr int kStagedThreads = 32 * (1 + kConsumers);
 
-__device__ unsigned int lbm_wait_timeouts;
-
 __device__ __forceinline__ void staged_row_coords(const Geo& g, int r, int& i0, int& i1) {
 #if LBM_DIM == 3
   i0 = r / g.n[1];
@@ -848,6 +850,200 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
 #endif
 }
 
+// ---------------------------------------------------------------------------
+// The closure step on the 5th-generation tensor cores.  A block of 128
+// threads takes 128 consecutive interior nodes per tile, one node per
+// thread: each thread pulls its node and computes its moments, the block's
+// normalised moments form the 128 x 16 A operand of the MLP's first layer in
+// shared memory, one thread issues the three layers' tcgen05 MMAs (FP32
+// accumulators in tensor memory, lbm_tc.cuh), each warp reads back its 32
+// rows, and every thread relaxes its node, adds the correction (with the
+// same guard as k_step_periodic_closure) and stores it.  Weights come from
+// the FP32 master block rounded to BF16 (the values of the warp kernel's
+// fragment copy); only the FP32 accumulation order inside a layer differs.
+#if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcCols = 128;
+struct ClosureTcSmem {
+  __nv_bfloat16 w1[lbm_mlp::H * lbm_mlp::IN];
+  __nv_bfloat16 w2[lbm_mlp::H * lbm_mlp::H];
+  __nv_bfloat16 w3[16 * lbm_mlp::H];
+  __nv_bfloat16 x[kTcRows * lbm_mlp::IN];
+  __nv_bfloat16 h[kTcRows * lbm_mlp::H];
+  float b1[lbm_mlp::H], b2[lbm_mlp::H], b3[lbm_mlp::OUT];
+  uint64_t bar;
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kTcRows) k_step_periodic_closure_tc(const S* __restrict__ f, S* __restrict__ fnew,
+                                                                     StepArgs a, ClosureArgs c) {
+  using namespace lbm_mlp;
+  using namespace lbm_tc;
+  __shared__ __align__(128) ClosureTcSmem sm;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char* w1b = reinterpret_cast<unsigned char*>(sm.w1);
+  unsigned char* w2b = reinterpret_cast<unsigned char*>(sm.w2);
+  unsigned char* w3b = reinterpret_cast<unsigned char*>(sm.w3);
+  unsigned char* xb = reinterpret_cast<unsigned char*>(sm.x);
+  unsigned char* hb = reinterpret_cast<unsigned char*>(sm.h);
+  for (int i = tid; i < H * IN; i += kTcRows) store_bf16(w1b, core_offset(i / IN, i % IN, IN), c.params[PW1 + i]);
+  for (int i = tid; i < H * H; i += kTcRows) store_bf16(w2b, core_offset(i / H, i % H, H), c.params[PW2 + i]);
+  for (int i = tid; i < 16 * H; i += kTcRows) {
+    const int r = i / H, k = i % H;
+    store_bf16(w3b, core_offset(r, k, H), r < OUT ? c.params[PW3 + r * H + k] : 0.0f);
+  }
+  for (int i = tid; i < H; i += kTcRows) {
+    sm.b1[i] = c.params[PB1 + i];
+    sm.b2[i] = c.params[PB2 + i];
+  }
+  for (int i = tid; i < OUT; i += kTcRows) sm.b3[i] = c.params[PB3 + i];
+  if (tid == 0) {
+    lbm::mbar_init(&sm.bar, 1);
+    lbm::mbar_init_fence();
+  }
+  if (warp == 0) tmem_alloc(&sm.tmem_base, kTcCols);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = sm.tmem_base;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  const uint32_t xa = lbm::smem_addr(sm.x), ha = lbm::smem_addr(sm.h);
+  const uint32_t w1a = lbm::smem_addr(sm.w1), w2a = lbm::smem_addr(sm.w2), w3a = lbm::smem_addr(sm.w3);
+  const Geo& g = a.g;
+  uint32_t phase = 0;
+  bool ok = true;
+  const long long tiles = (c.nodes + kTcRows - 1) / kTcRows;
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long node = tile * kTcRows + tid;
+    const bool active = node < c.nodes;
+    int idx[3] = {0, 0, 0};
+    long long q = active ? node : 0;
+    for (int d = LBM_DIM - 1; d >= 0; --d) {
+      idx[d] = (int)(q % g.n[d]) + g.h[d];
+      q /= g.n[d];
+    }
+    const long long o = lbm::node_offset(g, idx[0], idx[1], idx[2]);
+    R gv[LBM_Q], m[LBM_Q];
+    if (active) {
+      long long off0[2 * LBM_VMAX + 1], off1[2 * LBM_VMAX + 1], off2[2 * LBM_VMAX + 1];
+#pragma unroll
+      for (int s = -LBM_VMAX; s <= LBM_VMAX; ++s) {
+        off0[s + LBM_VMAX] = LBM_DIM > 0 ? wrap_off(idx[0], s, g.n[0], g.h[0], g.stride[0]) : 0;
+        off1[s + LBM_VMAX] = LBM_DIM > 1 ? wrap_off(idx[1], s, g.n[1], g.h[1], g.stride[1]) : 0;
+        off2[s + LBM_VMAX] = LBM_DIM > 2 ? wrap_off(idx[2], s, g.n[2], g.h[2], g.stride[2]) : 0;
+      }
+#define LBM_PULL_TC(k, vx, vy, vz)                                                              \
+  gv[k] = (R)Store<S>::load(f + o + (long long)(k) * g.vstride + off0[(vx) + LBM_VMAX] +        \
+                            off1[(vy) + LBM_VMAX] + off2[(vz) + LBM_VMAX]);
+      LBM_FOR_EACH_V(LBM_PULL_TC)
+#undef LBM_PULL_TC
+      lbm_moments<R>(gv, m);
+    } else {
+#pragma unroll
+      for (int k = 0; k < LBM_Q; ++k) m[k] = (R)0;
+    }
+    // this node's normalised pre-collision moments: row tid of the A operand
+#pragma unroll
+    for (int k = 0; k < IN; ++k) {
+      float v = 0.0f;
+      if (k < LBM_Q && active)
+        v = ((float)m[k] + (float)lbm_dev_mref[k < LBM_Q ? k : 0] - c.mu_in[k]) * c.isig_in[k];
+      store_bf16(xb, core_offset(tid, k, IN), v);
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after_sync();
+      mma_bf16(tmem, smem_desc(xa, 128, (IN / 8) * 128), smem_desc(w1a, 128, (IN / 8) * 128),
+               instr_desc(kTcRows, H), 0);
+      mma_commit(&sm.bar);
+    }
+    if (!(ok = wait_mma(&sm.bar, phase))) break;
+    fence_after_sync();
+#pragma unroll
+    for (int cc = 0; cc < H; cc += 16) {
+      float v[16];
+      tmem_ld16(tmem + lane_base + (uint32_t)cc, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, cc + j, H), silu(v[j] + sm.b1[cc + j]));
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after_sync();
+#pragma unroll
+      for (int kc = 0; kc < H / 16; ++kc)
+        mma_bf16(tmem + 64, smem_desc(ha + kc * 256, 128, (H / 8) * 128),
+                 smem_desc(w2a + kc * 256, 128, (H / 8) * 128), instr_desc(kTcRows, H), kc > 0);
+      mma_commit(&sm.bar);
+    }
+    if (!(ok = wait_mma(&sm.bar, phase))) break;
+    fence_after_sync();
+#pragma unroll
+    for (int cc = 0; cc < H; cc += 16) {
+      float v[16];
+      tmem_ld16(tmem + lane_base + 64u + (uint32_t)cc, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, cc + j, H), silu(v[j] + sm.b2[cc + j]));
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after_sync();
+#pragma unroll
+      for (int kc = 0; kc < H / 16; ++kc)
+        mma_bf16(tmem, smem_desc(ha + kc * 256, 128, (H / 8) * 128), smem_desc(w3a + kc * 256, 128, (H / 8) * 128),
+                 instr_desc(kTcRows, 16), kc > 0);
+      mma_commit(&sm.bar);
+    }
+    if (!(ok = wait_mma(&sm.bar, phase))) break;
+    fence_after_sync();
+    float y[16];
+    tmem_ld16(tmem + lane_base, y);
+    if (active) {
+      R pre[LBM_Q - LBM_NCONS];
+#pragma unroll
+      for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) pre[j] = m[LBM_NCONS + j];
+      lbm_relax<R>(m, a.prm);
+      float corr[LBM_Q - LBM_NCONS];
+      float change = 0.0f;
+#pragma unroll
+      for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) {
+        corr[j] = (y[j] + sm.b3[j]) * c.sig_out[j] + c.mu_out[j];
+        change = fmaxf(change, fabsf((float)(m[LBM_NCONS + j] - pre[j])));
+      }
+      bool keep = true;
+      if (c.guard_ratio > 0.0f) {
+        const float limit = c.guard_ratio * change + c.guard_floor;
+#pragma unroll
+        for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) keep = keep && fabsf(corr[j]) <= limit;  // false for NaN
+      }
+      if (keep) {
+#pragma unroll
+        for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) m[LBM_NCONS + j] += (R)corr[j];
+      } else if (c.fallbacks) {
+        atomicAdd(c.fallbacks, 1);
+      }
+      lbm_populations<R>(m, gv);
+#pragma unroll
+      for (int k = 0; k < LBM_Q; ++k) Store<S>::store(fnew + o + (long long)k * g.vstride, gv[k]);
+    }
+    fence_before_sync();
+    __syncthreads();
+  }
+  if (!ok && tid == 0) atomicAdd(&lbm_wait_timeouts, 1u);
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    tmem_dealloc(tmem, kTcCols);
+  }
+}
+#endif
+
 __global__ void __launch_bounds__(LBM_BLOCK) k_transport(const S* __restrict__ f, S* __restrict__ fnew,
                                                          StepArgs a) {
   int i0, i1, i2;
@@ -1120,13 +1316,8 @@ int lbm_scheme_set_step_variant(int32_t variant) {
 
 int lbm_scheme_wait_timeouts(uint32_t* count) {
   if (!count) return lbm::fail(LBM_ERR_ARG, "lbm_scheme_wait_timeouts: NULL");
-#if LBM_HAS_PAIRS
   return lbm::cuda_check(cudaMemcpyFromSymbol(count, lbm_scheme::lbm_wait_timeouts, sizeof(uint32_t)),
                          "lbm_scheme_wait_timeouts");
-#else
-  *count = 0;
-  return LBM_OK;
-#endif
 }
 
 static int step_common(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, void* stream,
@@ -1323,16 +1514,34 @@ int lbm_source_term(double* m, const lbm_lattice* mlat, const double* prm, void*
   return lbm::launch_check("lbm_source_term");
 }
 
+static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, const void* wbf16,
+                          const float* params, const float* norm, const float* guard, int32_t* fallbacks,
+                          int32_t grid, void* stream, bool tc, const char* who);
+
 int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
                                        const void* wbf16, const float* params, const float* norm,
                                        const float* guard, int32_t* fallbacks, int32_t grid, void* stream) {
+  return closure_common(f, fnew, lat, prm, wbf16, params, norm, guard, fallbacks, grid, stream, false,
+                        "lbm_one_time_step_periodic_closure");
+}
+
+int lbm_one_time_step_periodic_closure_tc(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
+                                          const float* params, const float* norm, const float* guard,
+                                          int32_t* fallbacks, void* stream) {
+  return closure_common(f, fnew, lat, prm, nullptr, params, norm, guard, fallbacks, 0, stream, true,
+                        "lbm_one_time_step_periodic_closure_tc");
+}
+
+static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, const void* wbf16,
+                          const float* params, const float* norm, const float* guard, int32_t* fallbacks,
+                          int32_t grid, void* stream, bool tc, const char* who) {
   using namespace lbm_scheme;
-  const char* who = "lbm_one_time_step_periodic_closure";
   int rc = check_pop_lattice(lat, who);
   if (rc) return rc;
   if (LBM_Q > 16 || LBM_Q - LBM_NCONS > 8)
     return lbm::fail(LBM_ERR_UNSUPPORTED, "%s: the closure MLP takes at most 16 moments and 8 corrections", who);
-  if (!f || !fnew || f == fnew || !wbf16 || !params || !norm) return lbm::fail(LBM_ERR_ARG, "%s: bad pointers", who);
+  if (!f || !fnew || f == fnew || (!tc && !wbf16) || !params || !norm)
+    return lbm::fail(LBM_ERR_ARG, "%s: bad pointers", who);
   if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "%s: %d parameters expected", who, LBM_NPRM);
   StepArgs a = make_step_args(*lat, prm);
   ClosureArgs c;
@@ -1350,6 +1559,19 @@ int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_latt
   c.guard_ratio = guard ? guard[0] : 0.0f;
   c.guard_floor = guard ? guard[1] : 0.0f;
   c.fallbacks = fallbacks;
+#if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
+  if (tc) {
+    int dev = 0, sms = 0;
+    int rc2 = lbm::cuda_check(cudaGetDevice(&dev), who);
+    if (!rc2) rc2 = lbm::cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), who);
+    if (rc2) return rc2;
+    const long long tiles = (c.nodes + kTcRows - 1) / kTcRows;
+    // four blocks per SM hold 4 x 128 of the 512 tensor-memory columns
+    const long long blocks = tiles < 4LL * sms ? tiles : 4LL * sms;
+    k_step_periodic_closure_tc<<<(unsigned)blocks, kTcRows, 0, (cudaStream_t)stream>>>((const S*)f, (S*)fnew, a, c);
+    return lbm::launch_check(who);
+  }
+#endif
   const long long per = 16 * kClosureWarps;
   long long blocks = (c.nodes + per - 1) / per;
   if (grid > 0 && blocks > grid) blocks = grid;

@@ -582,6 +582,9 @@ class Simulation:
         if model is not None and (self.scheme.Tu is not None or self.scheme.source_terms):
             raise ValueError("the learned closure corrects the plain MRT relaxation only")
         self.closure = model
+        if not hasattr(self, "closure_kernel"):
+            # "tc": tcgen05 MMAs, 128 nodes per block; "warp": mma.sync, 16 nodes per warp
+            self.closure_kernel = "tc"
         if model is not None and getattr(self, "_fallbacks", None) is None:
             self._fallbacks = runtime.DeviceBuffer(4)
         if model is not None:
@@ -600,6 +603,12 @@ class Simulation:
 
     def _launch_step(self, F, Fnew, pp):
         model = getattr(self, "closure", None)
+        if model is not None and getattr(self, "closure_kernel", "tc") == "tc":
+            # the MLP on the 5th-generation tensor cores, one node per thread
+            self.module.call(self.module.lib.lbm_one_time_step_periodic_closure_tc(
+                F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.p.handle, model.norm_ptr(),
+                model.guard_ptr(), self._fallbacks.handle, self._stream))
+            return
         if model is not None:
             self.module.call(self.module.lib.lbm_one_time_step_periodic_closure(
                 F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.w.handle, model.mlp.p.handle,
@@ -828,7 +837,8 @@ class Simulation:
             rc = self._core.lbm_graph_end(self._stream, ctypes.byref(g))
         runtime.check(rc)
         self._graph = g
-        self._graph_key = (self._F.ptr, self._Fnew.ptr, tuple(prm), self._folded(), self.batch_boundary)
+        self._graph_key = (self._F.ptr, self._Fnew.ptr, tuple(prm), self._folded(), self.batch_boundary,
+                           getattr(self, "closure_kernel", None))
 
     def run(self, nsteps, graph=True):
         """Advance ``nsteps`` time steps (same result as calling one_time_step)."""
@@ -841,7 +851,8 @@ class Simulation:
                 self.one_time_step()
             return
         prm = self._prm()
-        if self._graph_key != (self._F.ptr, self._Fnew.ptr, tuple(prm), self._folded(), self.batch_boundary):
+        if self._graph_key != (self._F.ptr, self._Fnew.ptr, tuple(prm), self._folded(), self.batch_boundary,
+                               getattr(self, "closure_kernel", None)):
             self._capture(prm)
         for _ in range(nsteps // 2):
             runtime.check(self._core.lbm_graph_launch(self._graph, self._stream))

@@ -32,15 +32,42 @@ def _moments(sim):
     return np.array([sim.m[k] for k in range(sim.scheme.nv)])
 
 
-def test_zero_network_equals_plain_step():
+@pytest.mark.parametrize("kernel", ["tc", "warp"])
+def test_zero_network_equals_plain_step(kernel):
     d = W.shear_layer(n=64, nu=1e-3)
     a = Simulation(d, dtype="float32")
     b = Simulation(d, dtype="float32")
     p = np.zeros_like(init_params(0))
     b.set_closure(ClosureModel(p, _norm()))
+    b.closure_kernel = kernel
     a.run(25)
     b.run(25)
     assert np.array_equal(_moments(a), _moments(b))
+
+
+def test_tensor_memory_step_equals_warp_step():
+    """The tcgen05 closure step (128 nodes per block, accumulators in tensor
+    memory) against the warp-level one on a random network: the same run up
+    to the FP32 accumulation order inside a layer (a hidden activation may
+    round to the neighbouring BF16 value), and no wait gives up."""
+    import ctypes
+    d = W.shear_layer(n=96, nu=1e-3, seed=6)
+    runs = []
+    for kernel in ("tc", "warp"):
+        sim = Simulation(d, dtype="float32")
+        model = ClosureModel(init_params(4), _norm(scale_out=1e-4))
+        model.guard[0] = 0.0  # guard off: a random network's corrections are not judged here
+        sim.set_closure(model)
+        sim.closure_kernel = kernel
+        sim.run(20)
+        runs.append(_moments(sim))
+        count = ctypes.c_uint32()
+        sim.module.call(sim.module.lib.lbm_scheme_wait_timeouts(ctypes.byref(count)))
+        assert count.value == 0 and sim.closure_fallbacks() == 0
+        sim.free()
+    tc, warp = runs
+    for k in range(tc.shape[0]):
+        assert np.abs(tc[k] - warp[k]).max() <= 1e-5 * max(np.abs(warp[k]).max(), 1e-3), k
 
 
 def test_closure_step_equals_relaxation_plus_network():
@@ -79,8 +106,9 @@ def test_closure_conserves_mass_and_momentum():
     assert np.all(np.abs(c1[1:] - c0[1:]) < 1e-6 * abs(c0[0]))
 
 
+@pytest.mark.parametrize("kernel", ["tc", "warp"])
 @pytest.mark.parametrize("bad", ["nan", "huge"])
-def test_guard_keeps_the_plain_collision_for_a_broken_network(bad):
+def test_guard_keeps_the_plain_collision_for_a_broken_network(bad, kernel):
     """A network whose outputs are not finite (NaN weights) or absurdly large
     (weights scaled by 1e6) trips the fused step's guard at every node: each
     node keeps the plain MRT collision, so the run equals the plain run bit
@@ -91,6 +119,7 @@ def test_guard_keeps_the_plain_collision_for_a_broken_network(bad):
     p = init_params(11).astype(np.float32)
     p = np.full_like(p, np.nan) if bad == "nan" else p * 1e6
     b.set_closure(ClosureModel(p, _norm(scale_out=1e-3)))
+    b.closure_kernel = kernel
     a.run(12)
     b.run(12)
     assert np.array_equal(_moments(a), _moments(b))

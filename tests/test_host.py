@@ -159,7 +159,7 @@ def runtime_scheme_symbols():
             "lbm_ensemble_step", "lbm_ensemble_step_pairs", "lbm_one_time_step_periodic_closure",
             "lbm_f2m_conserved", "lbm_source_term", "lbm_scheme_set_step_variant", "lbm_scheme_wait_timeouts",
             "lbm_init_conserved", "lbm_f2m_conserved_dense",
-            "lbm_one_time_step_walls"}
+            "lbm_one_time_step_walls", "lbm_one_time_step_periodic_closure_tc"}
 
 
 def test_scheme_module_builds_and_exports_header():
