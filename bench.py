@@ -345,8 +345,8 @@ def main():
     ap.add_argument("--workload", default="tgv", choices=["tgv", "cylinder", "karman", "cavity3d", "cavity", "closure"],
                     help="tgv: the headline D3Q19 workload; cylinder / karman / cavity3d / cavity (D2Q9 n^2): "
                          "the bounded flows; closure: the Re 30 000 shear layer n^2 with the learned closure")
-    ap.add_argument("--closure-kernel", default="tc", choices=["tc", "warp"],
-                    help="closure workload: tcgen05 MMAs (tc) or warp-level mma.sync (warp)")
+    ap.add_argument("--closure-kernel", default="auto", choices=["auto", "tc", "warp"],
+                    help="closure workload: tcgen05 MMAs (tc), warp-level mma.sync (warp), or by grid size (auto)")
     ap.add_argument("--step-variant", type=int, default=0, choices=[0, 1],
                     help="16-bit periodic steps: 1 staged kernel where rows fit, 0 direct-load kernel")
     ap.add_argument("--fp64-form", default="parity", choices=["parity", "exact"],
@@ -397,7 +397,8 @@ def main():
         sim = Simulation(study_dicos(100000, n), dtype=args.dtype)
         sim.set_closure(ClosureModel.load(DEFAULT_MODEL))
         sim.closure_kernel = args.closure_kernel
-        desc = f"D2Q9 MRT double shear layer {n}^2, Re 30 000, learned closure ({args.closure_kernel} kernel)"
+        kernel = "tc" if sim._closure_on_tensor_cores() else "warp"
+        desc = f"D2Q9 MRT double shear layer {n}^2, Re 30 000, learned closure ({kernel} kernel)"
     elif args.workload == "cavity":
         sim = Simulation(W.cavity(n=n), dtype=args.dtype, parity=parity)
         desc = f"D2Q9 MRT lid-driven cavity {n}^2 (bounce-back walls, moving lid)"
@@ -410,7 +411,7 @@ def main():
     buf_bytes = sim._lat.elements * BYTES_PER_VALUE[args.dtype]
     # kernels per step: the step, plus the ghost refresh and the boundary launches
     launches_per_step = sim.launches_per_step()
-    step_kernel = ("lbm_scheme::k_step_periodic_closure" + ("_tc" if args.closure_kernel == "tc" else "")
+    step_kernel = ("lbm_scheme::k_step_periodic_closure" + ("_tc" if sim._closure_on_tensor_cores() else "")
                    if args.workload == "closure"
                    else "lbm_scheme::k_step_walls" if sim._folded()
                    else "lbm_scheme::k_step_periodic_pairs" if sim.periodic and args.dtype in ("float16", "bfloat16")

@@ -437,6 +437,15 @@ int lbm_one_time_step_walls(const void* f, void* fnew, const lbm_lattice* lat, c
  * (default) the direct-load kernels; both give the same results bit for bit.
  * No reference counterpart. */
 int lbm_scheme_set_step_variant(int32_t variant);
+/* Blocks per SM of the tensor-core closure step
+ * (lbm_one_time_step_periodic_closure_tc): 0 (default) takes the bound set
+ * by the kernel's registers and shared memory, 1..8 a fixed count.  Either
+ * is capped at 8, the tensor-memory allocations of 64 columns an SM holds at
+ * once.  No reference counterpart. */
+int lbm_scheme_set_closure_tc_occupancy(int32_t blocks_per_sm);
+/* The resource bound for the current device and the blocks per SM the
+ * launch uses. */
+int lbm_scheme_closure_tc_occupancy(int32_t* bound, int32_t* used);
 /* Number of bounded waits of this module's kernels that gave up (0 in a
  * healthy run; a kernel whose wait times out leaves without completing). */
 int lbm_scheme_wait_timeouts(uint32_t* count);

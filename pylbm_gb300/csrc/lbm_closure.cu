@@ -411,8 +411,8 @@ int lbm_mlp_forward_tc(const void* x, int32_t n, const float* params, float* y, 
   if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "lbm_mlp_forward_tc");
   if (rc) return rc;
   const int tiles = (n + lbm_mlp_tc::kRows - 1) / lbm_mlp_tc::kRows;
-  // four blocks per SM hold 4 x 128 of the 512 tensor-memory columns
-  const int blocks = tiles < 4 * sms ? tiles : 4 * sms;
+  // eight blocks per SM hold 8 x 64 of the 512 tensor-memory columns
+  const int blocks = tiles < 8 * sms ? tiles : 8 * sms;
   lbm_mlp_tc::k_mlp_forward_tc<<<blocks, lbm_mlp_tc::kThreads, 0, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)x, n, params, y);
   return launch_check("lbm_mlp_forward_tc");

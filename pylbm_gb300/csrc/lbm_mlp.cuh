@@ -70,6 +70,10 @@ __device__ __forceinline__ float sigmoidf_(float z) { return fmaf(0.5f, tanh_app
 
 __device__ __forceinline__ float silu(float z) { return z * sigmoidf_(z); }
 
+struct Silu {
+  __device__ __forceinline__ float operator()(float z) const { return silu(z); }
+};
+
 __device__ __forceinline__ float silu_grad(float z) {
   const float s = sigmoidf_(z);
   return s * (1.0f + z * (1.0f - s));

@@ -11,9 +11,10 @@
 // arithmetic per element is that of the warp-level path (lbm_mlp.cuh); only
 // the order of the FP32 accumulation inside a layer may differ.
 //
-// Tensor memory: 128 columns per block (layer 1 and 3 accumulators share
-// columns 0..63, layer 2 uses 64..127), allocated by warp 0 at the start and
-// freed at the end.  Every mbarrier wait is bounded in time; a block whose
+// Tensor memory: 64 columns per block, allocated by warp 0 at the start and
+// freed at the end; the three layers' accumulators reuse them (every thread
+// has read a layer's columns before the barrier that precedes the next
+// layer's MMA).  Every mbarrier wait is bounded in time; a block whose
 // wait gives up leaves after all its threads agree (no partial barrier) and
 // counts the timeout.
 #pragma once
@@ -29,7 +30,7 @@ using namespace lbm_tc;
 
 constexpr int kRows = 128;         // samples per tile (MMA M)
 constexpr int kThreads = 128;      // one thread per sample row
-constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kTmemCols = 64;
 constexpr int kN3 = 16;            // layer-3 outputs padded to the MMA's smallest N for M = 128
 
 // waits that gave up (0 in a healthy run), read by lbm_mlp_tc_timeouts
@@ -56,12 +57,9 @@ __global__ void __launch_bounds__(kThreads) k_mlp_forward_tc(const __nv_bfloat16
   unsigned char* xb = reinterpret_cast<unsigned char*>(sm.x);
   unsigned char* hb = reinterpret_cast<unsigned char*>(sm.h);
   // weights: the BF16 rounding of the FP32 master block (as lbm_mlp_sync_weights)
-  for (int i = tid; i < H * IN; i += kThreads) store_bf16(w1b, core_offset(i / IN, i % IN, IN), params[PW1 + i]);
-  for (int i = tid; i < H * H; i += kThreads) store_bf16(w2b, core_offset(i / H, i % H, H), params[PW2 + i]);
-  for (int i = tid; i < kN3 * H; i += kThreads) {
-    const int r = i / H, k = i % H;
-    store_bf16(w3b, core_offset(r, k, H), r < OUT ? params[PW3 + r * H + k] : 0.0f);
-  }
+  stage_bf16(w1b, params + PW1, H, H, IN, tid, kThreads);
+  stage_bf16(w2b, params + PW2, H, H, H, tid, kThreads);
+  stage_bf16(w3b, params + PW3, kN3, OUT, H, tid, kThreads);
   for (int i = tid; i < H; i += kThreads) {
     sm.b1[i] = params[PB1 + i];
     sm.b2[i] = params[PB2 + i];
@@ -71,13 +69,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_forward_tc(const __nv_bfloat16
     lbm::mbar_init(&sm.bar, 1);
     lbm::mbar_init_fence();
   }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     lbm::smem_addr(&sm.tmem_base)),
-                 "r"(kTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
+  if (warp == 0) tmem_alloc(&sm.tmem_base, kTmemCols);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
@@ -112,34 +104,22 @@ __global__ void __launch_bounds__(kThreads) k_mlp_forward_tc(const __nv_bfloat16
     }
     if (!(ok = wait_mma(&sm.bar, phase))) break;
     fence_after_sync();
-#pragma unroll
-    for (int c = 0; c < H; c += 16) {
-      float v[16];
-      tmem_ld16(tmem + lane_base + (uint32_t)c, v);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, c + j, H), lbm_mlp::silu(v[j] + sm.b1[c + j]));
-    }
+    epilogue_bf16<H>(tmem + lane_base, sm.b1, hb, tid, Silu());
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
-    // layer 2: D[64:128) = H1 (128 x 64) W2^T, four K = 16 steps
+    // layer 2: D[0:64) = H1 (128 x 64) W2^T, four K = 16 steps
     if (tid == 0) {
       fence_after_sync();
 #pragma unroll
       for (int kc = 0; kc < H / 16; ++kc)
-        mma_bf16(tmem + 64, smem_desc(ha + kc * 256, 128, (H / 8) * 128), smem_desc(w2a + kc * 256, 128, (H / 8) * 128),
+        mma_bf16(tmem, smem_desc(ha + kc * 256, 128, (H / 8) * 128), smem_desc(w2a + kc * 256, 128, (H / 8) * 128),
                  instr_desc(kRows, H), kc > 0);
       mma_commit(&sm.bar);
     }
     if (!(ok = wait_mma(&sm.bar, phase))) break;
     fence_after_sync();
-#pragma unroll
-    for (int c = 0; c < H; c += 16) {
-      float v[16];
-      tmem_ld16(tmem + lane_base + 64u + (uint32_t)c, v);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, c + j, H), lbm_mlp::silu(v[j] + sm.b2[c + j]));
-    }
+    epilogue_bf16<H>(tmem + lane_base, sm.b2, hb, tid, Silu());
     fence_async_smem();
     fence_before_sync();
     __syncthreads();

@@ -863,7 +863,7 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
 // fragment copy); only the FP32 accumulation order inside a layer differs.
 #if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
 constexpr int kTcRows = 128;
-constexpr uint32_t kTcCols = 128;
+constexpr uint32_t kTcCols = 64;  // the three layers reuse columns 0..63
 struct ClosureTcSmem {
   __nv_bfloat16 w1[lbm_mlp::H * lbm_mlp::IN];
   __nv_bfloat16 w2[lbm_mlp::H * lbm_mlp::H];
@@ -886,12 +886,9 @@ __global__ void __launch_bounds__(kTcRows) k_step_periodic_closure_tc(const S* _
   unsigned char* w3b = reinterpret_cast<unsigned char*>(sm.w3);
   unsigned char* xb = reinterpret_cast<unsigned char*>(sm.x);
   unsigned char* hb = reinterpret_cast<unsigned char*>(sm.h);
-  for (int i = tid; i < H * IN; i += kTcRows) store_bf16(w1b, core_offset(i / IN, i % IN, IN), c.params[PW1 + i]);
-  for (int i = tid; i < H * H; i += kTcRows) store_bf16(w2b, core_offset(i / H, i % H, H), c.params[PW2 + i]);
-  for (int i = tid; i < 16 * H; i += kTcRows) {
-    const int r = i / H, k = i % H;
-    store_bf16(w3b, core_offset(r, k, H), r < OUT ? c.params[PW3 + r * H + k] : 0.0f);
-  }
+  stage_bf16(w1b, c.params + PW1, H, H, IN, tid, kTcRows);
+  stage_bf16(w2b, c.params + PW2, H, H, H, tid, kTcRows);
+  stage_bf16(w3b, c.params + PW3, 16, OUT, H, tid, kTcRows);
   for (int i = tid; i < H; i += kTcRows) {
     sm.b1[i] = c.params[PB1 + i];
     sm.b2[i] = c.params[PB2 + i];
@@ -943,12 +940,16 @@ __global__ void __launch_bounds__(kTcRows) k_step_periodic_closure_tc(const S* _
       for (int k = 0; k < LBM_Q; ++k) m[k] = (R)0;
     }
     // this node's normalised pre-collision moments: row tid of the A operand
+    {
+      float v[IN];
 #pragma unroll
-    for (int k = 0; k < IN; ++k) {
-      float v = 0.0f;
-      if (k < LBM_Q && active)
-        v = ((float)m[k] + (float)lbm_dev_mref[k < LBM_Q ? k : 0] - c.mu_in[k]) * c.isig_in[k];
-      store_bf16(xb, core_offset(tid, k, IN), v);
+      for (int k = 0; k < IN; ++k) {
+        v[k] = 0.0f;
+        if (k < LBM_Q && active)
+          v[k] = ((float)m[k < LBM_Q ? k : 0] + (float)lbm_dev_mref[k < LBM_Q ? k : 0] - c.mu_in[k]) * c.isig_in[k];
+      }
+      store8_bf16(xb, core_offset(tid, 0, IN), v);
+      store8_bf16(xb, core_offset(tid, 8, IN), v + 8);
     }
     fence_async_smem();
     fence_before_sync();
@@ -961,13 +962,7 @@ __global__ void __launch_bounds__(kTcRows) k_step_periodic_closure_tc(const S* _
     }
     if (!(ok = wait_mma(&sm.bar, phase))) break;
     fence_after_sync();
-#pragma unroll
-    for (int cc = 0; cc < H; cc += 16) {
-      float v[16];
-      tmem_ld16(tmem + lane_base + (uint32_t)cc, v);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, cc + j, H), silu(v[j] + sm.b1[cc + j]));
-    }
+    epilogue_bf16<H>(tmem + lane_base, sm.b1, hb, tid, Silu());
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
@@ -975,19 +970,13 @@ __global__ void __launch_bounds__(kTcRows) k_step_periodic_closure_tc(const S* _
       fence_after_sync();
 #pragma unroll
       for (int kc = 0; kc < H / 16; ++kc)
-        mma_bf16(tmem + 64, smem_desc(ha + kc * 256, 128, (H / 8) * 128),
+        mma_bf16(tmem, smem_desc(ha + kc * 256, 128, (H / 8) * 128),
                  smem_desc(w2a + kc * 256, 128, (H / 8) * 128), instr_desc(kTcRows, H), kc > 0);
       mma_commit(&sm.bar);
     }
     if (!(ok = wait_mma(&sm.bar, phase))) break;
     fence_after_sync();
-#pragma unroll
-    for (int cc = 0; cc < H; cc += 16) {
-      float v[16];
-      tmem_ld16(tmem + lane_base + 64u + (uint32_t)cc, v);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) store_bf16(hb, core_offset(tid, cc + j, H), silu(v[j] + sm.b2[cc + j]));
-    }
+    epilogue_bf16<H>(tmem + lane_base, sm.b2, hb, tid, Silu());
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
@@ -1308,6 +1297,73 @@ int lbm_scheme_describe(int32_t* nv, int32_t* dim, int32_t* nprm, int32_t* stora
 // staged kernel where the rows fit
 static int g_step_variant = 0;
 
+#if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
+// blocks per SM of the tensor-core closure step: 0 = the resource bound
+// below, else a fixed count; always within the 512 / kTcCols tensor-memory
+// allocations an SM can hold at once, so no allocation waits on another
+// block.  The bound comes from the kernel's registers and shared memory and
+// the SM's limits (the runtime's occupancy query answers 1 block per SM for
+// this kernel although several run side by side).
+static int g_closure_tc_occupancy = 0;
+
+static int closure_tc_blocks_per_sm(int dev, int* used, int* bound_out) {
+  static int cache[64];  // the resource bound per device ordinal, 0 until computed
+  int bound = dev >= 0 && dev < 64 ? cache[dev] : 0;
+  if (bound == 0) {
+    const char* who = "closure_tc_blocks_per_sm";
+    cudaFuncAttributes fa;
+    int regs = 0, smem = 0, reserved = 0, threads = 0;
+    int rc = lbm::cuda_check(cudaFuncGetAttributes(&fa, lbm_scheme::k_step_periodic_closure_tc), who);
+    if (!rc) rc = lbm::cuda_check(cudaDeviceGetAttribute(&regs, cudaDevAttrMaxRegistersPerMultiprocessor, dev), who);
+    if (!rc)
+      rc = lbm::cuda_check(cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev), who);
+    if (!rc) rc = lbm::cuda_check(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev), who);
+    if (!rc)
+      rc = lbm::cuda_check(cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev), who);
+    if (rc) return rc;
+    const int rows = lbm_scheme::kTcRows;
+    const int regs_block = ((fa.numRegs + 7) / 8) * 8 * rows;  // registers are allocated 256 per warp
+    bound = (int)(512 / lbm_scheme::kTcCols);
+    if (regs_block > 0 && regs / regs_block < bound) bound = regs / regs_block;
+    if (smem / (int)(fa.sharedSizeBytes + reserved) < bound) bound = smem / (int)(fa.sharedSizeBytes + reserved);
+    if (threads / rows < bound) bound = threads / rows;
+    if (bound < 1) bound = 1;
+    if (dev >= 0 && dev < 64) cache[dev] = bound;
+  }
+  int n = g_closure_tc_occupancy > 0 ? g_closure_tc_occupancy : bound;
+  if (n > (int)(512 / lbm_scheme::kTcCols)) n = (int)(512 / lbm_scheme::kTcCols);
+  if (used) *used = n;
+  if (bound_out) *bound_out = bound;
+  return LBM_OK;
+}
+#endif
+
+int lbm_scheme_set_closure_tc_occupancy(int32_t blocks_per_sm) {
+  if (blocks_per_sm < 0 || blocks_per_sm > 8)
+    return lbm::fail(LBM_ERR_ARG, "lbm_scheme_set_closure_tc_occupancy: %d (0..8)", blocks_per_sm);
+#if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
+  g_closure_tc_occupancy = blocks_per_sm;
+  return LBM_OK;
+#else
+  return lbm::fail(LBM_ERR_UNSUPPORTED, "lbm_scheme_set_closure_tc_occupancy: no closure step in this scheme");
+#endif
+}
+
+int lbm_scheme_closure_tc_occupancy(int32_t* bound, int32_t* used) {
+  if (!bound || !used) return lbm::fail(LBM_ERR_ARG, "lbm_scheme_closure_tc_occupancy: NULL");
+#if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
+  int dev = 0, q = 0, u = 0;
+  int rc = lbm::cuda_check(cudaGetDevice(&dev), "lbm_scheme_closure_tc_occupancy");
+  if (!rc) rc = closure_tc_blocks_per_sm(dev, &u, &q);
+  if (rc) return rc;
+  *bound = q;
+  *used = u;
+  return LBM_OK;
+#else
+  return lbm::fail(LBM_ERR_UNSUPPORTED, "lbm_scheme_closure_tc_occupancy: no closure step in this scheme");
+#endif
+}
+
 int lbm_scheme_set_step_variant(int32_t variant) {
   if (variant < 0 || variant > 1) return lbm::fail(LBM_ERR_ARG, "lbm_scheme_set_step_variant: %d", variant);
   g_step_variant = variant;
@@ -1565,9 +1621,12 @@ static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, con
     int rc2 = lbm::cuda_check(cudaGetDevice(&dev), who);
     if (!rc2) rc2 = lbm::cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), who);
     if (rc2) return rc2;
+    int per_sm = 0;
+    rc2 = closure_tc_blocks_per_sm(dev, &per_sm, nullptr);
+    if (rc2) return rc2;
     const long long tiles = (c.nodes + kTcRows - 1) / kTcRows;
-    // four blocks per SM hold 4 x 128 of the 512 tensor-memory columns
-    const long long blocks = tiles < 4LL * sms ? tiles : 4LL * sms;
+    const long long cap = (long long)per_sm * sms;
+    const long long blocks = tiles < cap ? tiles : cap;
     k_step_periodic_closure_tc<<<(unsigned)blocks, kTcRows, 0, (cudaStream_t)stream>>>((const S*)f, (S*)fnew, a, c);
     return lbm::launch_check(who);
   }

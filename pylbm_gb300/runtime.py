@@ -426,7 +426,8 @@ class SchemeModule:
         self.storage = storage
         self.compute = compute
         text = source_obj.module_source(storage, compute)
-        deps = "".join(open(os.path.join(CSRC, f)).read() for f in ("lbm_common.cuh", "scheme_kernels.cuh"))
+        deps = "".join(open(os.path.join(CSRC, f)).read()
+                       for f in ("lbm_common.cuh", "lbm_mlp.cuh", "lbm_tc.cuh", "scheme_kernels.cuh"))
         deps += open(os.path.join(INCLUDE, "lbm_gb300.h")).read()
         flags = list(getattr(source_obj, "nvcc_flags", []))
         key = hashlib.sha256((text + deps + " ".join(ARCH_FLAGS + flags)).encode()).hexdigest()[:20]
@@ -475,6 +476,8 @@ class SchemeModule:
         _sig(lib, "lbm_f2m_conserved_dense", I32, [P, LP, P, P])
         _sig(lib, "lbm_scheme_set_step_variant", I32, [I32])
         _sig(lib, "lbm_scheme_wait_timeouts", I32, [ctypes.POINTER(ctypes.c_uint32)])
+        _sig(lib, "lbm_scheme_set_closure_tc_occupancy", I32, [I32])
+        _sig(lib, "lbm_scheme_closure_tc_occupancy", I32, [ctypes.POINTER(ctypes.c_int32)] * 2)
         _sig(lib, "lbm_ensemble_step", I32, [P, P, P, I32, I32, I32, I32, I32, P])
         _sig(lib, "lbm_ensemble_step_pairs", I32, [P, P, P, I32, I32, I32, I32, I32, P])
         _sig(lib, "lbm_one_time_step_periodic_closure", I32, [P, P, LP, P, P, P, P, P, P, I32, P])

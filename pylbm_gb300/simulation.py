@@ -583,8 +583,11 @@ class Simulation:
             raise ValueError("the learned closure corrects the plain MRT relaxation only")
         self.closure = model
         if not hasattr(self, "closure_kernel"):
-            # "tc": tcgen05 MMAs, 128 nodes per block; "warp": mma.sync, 16 nodes per warp
-            self.closure_kernel = "tc"
+            # "tc": tcgen05 MMAs, 128 nodes per block; "warp": mma.sync, 16 nodes
+            # per warp; "auto": the tensor-core step from 2^18 interior nodes on
+            # (the warp kernel is faster on smaller grids, where a block's
+            # set-up is not spread over enough tiles)
+            self.closure_kernel = "auto"
         if model is not None and getattr(self, "_fallbacks", None) is None:
             self._fallbacks = runtime.DeviceBuffer(4)
         if model is not None:
@@ -603,7 +606,7 @@ class Simulation:
 
     def _launch_step(self, F, Fnew, pp):
         model = getattr(self, "closure", None)
-        if model is not None and getattr(self, "closure_kernel", "tc") == "tc":
+        if model is not None and self._closure_on_tensor_cores():
             # the MLP on the 5th-generation tensor cores, one node per thread
             self.module.call(self.module.lib.lbm_one_time_step_periodic_closure_tc(
                 F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.p.handle, model.norm_ptr(),
@@ -616,6 +619,14 @@ class Simulation:
             return
         fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
         self.module.call(fn(F.handle, Fnew.handle, ctypes.byref(self._lat), pp, self._stream))
+
+    def _closure_on_tensor_cores(self):
+        kernel = getattr(self, "closure_kernel", "auto")
+        if kernel not in ("auto", "tc", "warp"):
+            raise ValueError(f"closure_kernel: {kernel!r} (auto, tc or warp)")
+        if kernel == "auto":
+            return int(np.prod(self.domain.shape_in)) >= 1 << 18
+        return kernel == "tc"
 
     def launches_per_step(self):
         """Kernel launches of one step: ghost refresh, boundary methods, step."""

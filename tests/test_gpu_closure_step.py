@@ -70,6 +70,51 @@ def test_tensor_memory_step_equals_warp_step():
         assert np.abs(tc[k] - warp[k]).max() <= 1e-5 * max(np.abs(warp[k]).max(), 1e-3), k
 
 
+def test_tensor_core_step_does_not_depend_on_blocks_per_sm():
+    """Tiles are independent: the tcgen05 closure step gives the same run bit
+    for bit whatever the number of blocks per SM (one block looping over
+    many tiles, or many blocks sharing an SM's tensor memory), and the
+    resource bound it takes by default is at least one block."""
+    import ctypes
+    d = W.shear_layer(n=160, nu=1e-3, seed=8)
+    runs = []
+    for occ in (0, 1, 3, 8):
+        sim = Simulation(d, dtype="float32")
+        model = ClosureModel(init_params(5), _norm(scale_out=1e-4))
+        model.guard[0] = 0.0
+        sim.set_closure(model)
+        sim.closure_kernel = "tc"
+        lib = sim.module.lib
+        sim.module.call(lib.lbm_scheme_set_closure_tc_occupancy(occ))
+        try:
+            sim.run(15)
+            runs.append(_moments(sim))
+            bound, used = ctypes.c_int32(), ctypes.c_int32()
+            sim.module.call(lib.lbm_scheme_closure_tc_occupancy(ctypes.byref(bound), ctypes.byref(used)))
+            assert 1 <= bound.value <= 8
+            assert used.value == (occ if occ else bound.value)
+        finally:
+            sim.module.call(lib.lbm_scheme_set_closure_tc_occupancy(0))
+            sim.free()
+    for r in runs[1:]:
+        assert np.array_equal(r, runs[0])
+
+
+def test_auto_closure_kernel_follows_grid_size():
+    small = Simulation(W.shear_layer(n=64, nu=1e-3), dtype="float32")
+    large = Simulation(W.shear_layer(n=512, nu=1e-3), dtype="float32")
+    model = ClosureModel(init_params(1), _norm(scale_out=1e-4))
+    for sim in (small, large):
+        sim.set_closure(model)
+        assert sim.closure_kernel == "auto"
+    assert not small._closure_on_tensor_cores() and large._closure_on_tensor_cores()
+    small.closure_kernel = "bogus"
+    with pytest.raises(ValueError):
+        small.one_time_step()
+    small.free()
+    large.free()
+
+
 def test_closure_step_equals_relaxation_plus_network():
     d = W.shear_layer(n=48, nu=1e-3, seed=4)
     sim = Simulation(d, dtype="float32")

@@ -159,7 +159,8 @@ def runtime_scheme_symbols():
             "lbm_ensemble_step", "lbm_ensemble_step_pairs", "lbm_one_time_step_periodic_closure",
             "lbm_f2m_conserved", "lbm_source_term", "lbm_scheme_set_step_variant", "lbm_scheme_wait_timeouts",
             "lbm_init_conserved", "lbm_f2m_conserved_dense",
-            "lbm_one_time_step_walls", "lbm_one_time_step_periodic_closure_tc"}
+            "lbm_one_time_step_walls", "lbm_one_time_step_periodic_closure_tc",
+            "lbm_scheme_set_closure_tc_occupancy", "lbm_scheme_closure_tc_occupancy"}
 
 
 def test_scheme_module_builds_and_exports_header():
