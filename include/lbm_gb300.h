@@ -252,13 +252,29 @@ typedef struct lbm_domain {
 #define LBM_ELEMENT_CIRCLE 1        /* p = cx, cy, radius; one label */
 #define LBM_ELEMENT_PARALLELOGRAM 2 /* p = point x, y, v1 x, y, v2 x, y; labels of the 4 edges */
 #define LBM_ELEMENT_SPHERE 3        /* p = cx, cy, cz, radius; one label (3D domains) */
+/* The kinds below take the constants of their ray equations from the host
+ * (pylbm_gb300/geometry.py ``device_params``), per element in p and per
+ * unique velocity u in vq[u]; the device repeats only the per-node terms. */
+#define LBM_ELEMENT_ELLIPSE 4   /* p = cx, cy, sxx, syy, sxy, det2 (syy X^2 + sxx Y^2 - sxy XY = det2);
+                                   vq[u][0] = the ray quadratic's coefficient; one label
+                                   (pylbm/elements/ellipse.py) */
+#define LBM_ELEMENT_TRIANGLE 5  /* p = point x, y, v1 x, y, v2 x, y; labels of the 3 edges
+                                   (pylbm/elements/triangle.py) */
+#define LBM_ELEMENT_ELLIPSOID 6 /* p = cx, cy, cz, cxx, cyy, czz, cxy, cyz, czx, d; vq[u] = the ray
+                                   quadratic's coefficient and the 3 factors of its linear one;
+                                   one label (pylbm/elements/ellipsoid.py) */
+#define LBM_ELEMENT_CYLINDER 7  /* p = center x, y, z, the inverse frame matrix (9, row-major), the
+                                   section (0 disc, 1 triangle, 2 square); vq[u] = velocity u in the
+                                   frame and, for the disc, the side's ray quadratic coefficient;
+                                   labels: the sides, bottom, top (pylbm/elements/cylinder.py) */
 
 typedef struct lbm_element {
   int32_t kind;
   int32_t isfluid;            /* 1: the element carves fluid out of solid */
-  int32_t label[4];
-  double p[8];
+  int32_t label[6];
+  double p[24];
   int32_t lo[3], hi[3];       /* halo-coordinate region [lo, hi) the element touches */
+  double vq[LBM_MAX_Q][4];    /* per unique velocity constants (kinds 4..7) */
 } lbm_element;
 
 /* in_or_out = -1 with 999 on the interior, distance = 999, flag = 999

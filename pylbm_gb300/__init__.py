@@ -9,7 +9,8 @@ from . import boundary as bc
 from .boundary import (AntiBounceBack, BounceBack, BouzidiAntiBounceBack, BouzidiBounceBack, Neumann, NeumannX,
                        NeumannY, NeumannZ)
 from .domain import Domain
-from .geometry import Circle, Parallelogram, Sphere
+from .geometry import (Circle, CylinderCircle, CylinderEllipse, CylinderTriangle, Ellipse, Ellipsoid, Parallelepiped,
+                       Parallelogram, Sphere, Triangle)
 from .output import H5File
 from .runtime import pinned_empty
 from .scheme import Scheme, SchemeError
@@ -18,6 +19,7 @@ from .stencil import Stencil
 
 __version__ = "0.1.0"
 
-__all__ = ["Simulation", "Scheme", "SchemeError", "Domain", "Stencil", "Circle", "Parallelogram", "Sphere",
+__all__ = ["Simulation", "Scheme", "SchemeError", "Domain", "Stencil", "Circle", "Ellipse", "Parallelogram", "Triangle",
+           "Sphere", "Ellipsoid", "CylinderCircle", "CylinderEllipse", "CylinderTriangle", "Parallelepiped",
            "H5File", "pinned_empty", "bc", "BounceBack", "AntiBounceBack", "BouzidiBounceBack", "BouzidiAntiBounceBack", "Neumann",
            "NeumannX", "NeumannY", "NeumannZ"]

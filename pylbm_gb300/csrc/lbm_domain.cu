@@ -121,6 +121,30 @@ __device__ __forceinline__ void region_node(const Region& r, long long t, int (&
   i[0] = r.lo[0] + (int)(q / n1);
 }
 
+// cxx X^2 + cyy Y^2 + czz Z^2 + cxy XY + cyz YZ + czx ZX, left to right
+// (ellipsoid coefficients p[3..8])
+__device__ __forceinline__ double quadric_form(const lbm_element& e, double X, double Y, double Z) {
+  return add(add(add(add(add(mul(e.p[3], mul(X, X)), mul(e.p[4], mul(Y, Y))), mul(e.p[5], mul(Z, Z))),
+                     mul(mul(e.p[6], X), Y)),
+                 mul(mul(e.p[7], Y), Z)),
+             mul(mul(e.p[8], Z), X));
+}
+
+// (x, y, z) in a cylinder's frame: the inverse frame matrix p[3..11] applied
+// to the offset from the centre p[0..2]
+__device__ __forceinline__ void to_frame(const lbm_element& e, double x, double y, double z, double (&f)[3]) {
+  const double xx = sub(x, e.p[0]), yy = sub(y, e.p[1]), zz = sub(z, e.p[2]);
+  for (int r = 0; r < 3; ++r)
+    f[r] = add(add(mul(e.p[3 + 3 * r], xx), mul(e.p[4 + 3 * r], yy)), mul(e.p[5 + 3 * r], zz));
+}
+
+// the cylinder's section in its frame: unit disc, unit triangle, unit square
+__device__ __forceinline__ bool section_inside(int section, double x, double y) {
+  if (section == 0) return add(mul(x, x), mul(y, y)) <= 1.0;
+  if (section == 1) return x >= 0 && y >= 0 && add(x, y) <= 1;
+  return x >= 0 && y >= 0 && x <= 1 && y <= 1;
+}
+
 __device__ __forceinline__ bool inside(const lbm_element& e, double x, double y, double z) {
   if (e.kind == LBM_ELEMENT_SPHERE) {
     const double px = sub(x, e.p[0]), py = sub(y, e.p[1]), pz = sub(z, e.p[2]);
@@ -130,19 +154,120 @@ __device__ __forceinline__ bool inside(const lbm_element& e, double x, double y,
     const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
     return add(mul(px, px), mul(py, py)) <= mul(e.p[2], e.p[2]);
   }
-  // parallelogram: barycentric coordinates in (v1, v2)
+  if (e.kind == LBM_ELEMENT_ELLIPSE) {
+    const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
+    return sub(add(mul(mul(px, px), e.p[3]), mul(mul(py, py), e.p[2])), mul(mul(px, py), e.p[4])) <= e.p[5];
+  }
+  if (e.kind == LBM_ELEMENT_ELLIPSOID) {
+    const double X = sub(x, e.p[0]), Y = sub(y, e.p[1]), Z = sub(z, e.p[2]);
+    return quadric_form(e, X, Y, Z) <= e.p[9];
+  }
+  if (e.kind == LBM_ELEMENT_CYLINDER) {
+    double f[3];
+    to_frame(e, x, y, z, f);
+    return section_inside((int)e.p[12], f[0], f[1]) && fabs(f[2]) <= 1.0;
+  }
+  // parallelogram and triangle: barycentric coordinates in (v1, v2)
   const double dx = sub(x, e.p[0]), dy = sub(y, e.p[1]);
   const double inv = dvd(1.0, sub(mul(e.p[2], e.p[5]), mul(e.p[3], e.p[4])));
   const double a = mul(sub(mul(dx, e.p[5]), mul(dy, e.p[4])), inv);
   const double bb = mul(sub(mul(dy, e.p[2]), mul(dx, e.p[3])), inv);
+  if (e.kind == LBM_ELEMENT_TRIANGLE) return a >= 0 && bb >= 0 && add(a, bb) <= 1;
   return a >= 0 && bb >= 0 && a <= 1 && bb <= 1;
 }
 
-// first crossing of the ray (x, y) + t v, t in (0, dmax], with the element
-// boundary: t (or -1) and the label of the crossed edge (or -1)
-// the ray (x, y, z) + t v against the sphere, as the host evaluates the
-// ellipsoid quadratic with the semi-axes r e_x, r e_y, r e_z (cross products,
-// then the quadratic's coefficients, term by term in the host's order)
+// First crossing of the ray (x, y[, z]) + t v, t in (0, dmax], with the
+// element boundary: t (or -1) and the label of the crossed edge (or -1).
+
+// roots of the ellipse rule (pylbm/elements/utils.py:93-150): the smallest
+// non-negative root of qa t^2 + qb t + qc, none when qa == 0
+__device__ __forceinline__ double ellipse_crossing(double px, double py, double vx, double vy, double sxx,
+                                                  double syy, double sxy, double det2, double qa, double dmax,
+                                                  int label, int& border) {
+  const double qb = sub(add(mul(mul(mul(2.0, px), vx), syy), mul(mul(mul(2.0, py), vy), sxx)),
+                        mul(add(mul(px, vy), mul(py, vx)), sxy));
+  const double qc = sub(sub(add(mul(mul(px, px), syy), mul(mul(py, py), sxx)), mul(mul(px, py), sxy)), det2);
+  const double disc = sub(mul(qb, qb), mul(mul(4.0, qa), qc));
+  const bool ok = disc >= 0;
+  const double root = __dsqrt_rn(ok ? disc : 0.0);
+  double t1 = kFar, t2 = kFar;
+  if (qa != 0) {
+    t1 = ok ? dvd(sub(-qb, root), mul(2.0, qa)) : kFar;
+    t2 = ok ? dvd(add(-qb, root), mul(2.0, qa)) : kFar;
+  }
+  if (t1 < 0) t1 = kFar;
+  if (t2 < 0) t2 = kFar;
+  double t = ok ? fmin(t1, t2) : -1.0;
+  if (t == kFar) t = -1.0;
+  border = -1;
+  if (t > 0 && t <= dmax) {
+    border = label;
+    return t;
+  }
+  return -1.0;
+}
+
+// segments q_k + s w_k, s in [0, 1], tried in order, a later one winning only
+// when strictly closer (pylbm/elements/utils.py:21-90)
+__device__ __forceinline__ double lines_crossing(double px, double py, double vx, double vy, int n,
+                                                const double (*q)[2], const double (*w)[2], const int* labels,
+                                                double dmax, int& border) {
+  double alpha = kFar;
+  border = -1;
+  for (int k = 0; k < n; ++k) {
+    const double det = sub(mul(vy, w[k][0]), mul(vx, w[k][1]));
+    if (det == 0) continue;
+    const double inv = dvd(1.0, det);
+    const double c1 = sub(q[k][0], px), c2 = sub(q[k][1], py);
+    const double t = mul(add(mul(-w[k][1], c1), mul(w[k][0], c2)), inv);
+    const double s = mul(add(mul(-vy, c1), mul(vx, c2)), inv);
+    if (t > 0 && s >= 0 && s <= 1 && t <= dmax && alpha > t) {
+      alpha = t;
+      border = labels[k];
+    }
+  }
+  if (alpha == kFar) {
+    border = -1;
+    return -1.0;
+  }
+  return alpha;
+}
+
+// the ellipsoid rule (pylbm/elements/utils.py:160-230): quadratic
+// coefficient qa and linear factors (bx, by, bz) of the ray, implicit-form
+// coefficients c[0..5] = cxx, cyy, czz, cxy, cyz, czx and right side dd
+__device__ __forceinline__ double quadric_crossing(double X, double Y, double Z, const double (&c)[6], double dd,
+                                                  double qa, double bx, double by, double bz, double dmax,
+                                                  int label, int& border) {
+  const double qb = add(add(mul(bx, X), mul(by, Y)), mul(bz, Z));
+  const double qc =
+      sub(add(add(add(add(add(mul(c[0], mul(X, X)), mul(c[1], mul(Y, Y))), mul(c[2], mul(Z, Z))), mul(mul(c[3], X), Y)),
+                  mul(mul(c[4], Y), Z)),
+              mul(mul(c[5], Z), X)),
+          dd);
+  double disc = sub(mul(qb, qb), mul(mul(4.0, qa), qc));
+  const bool ok = disc >= 0;
+  double t1 = kFar, t2 = kFar;
+  if (ok) {
+    disc = __dsqrt_rn(disc);
+    t1 = dvd(sub(-qb, disc), mul(2.0, qa));
+    t2 = dvd(add(-qb, disc), mul(2.0, qa));
+  }
+  if (t1 < 0) t1 = kFar;
+  if (t2 < 0) t2 = kFar;
+  double t = ok ? fmin(t1, t2) : -1.0;
+  if (t == kFar) t = -1.0;
+  border = -1;
+  if (t > 0 && t <= dmax) {
+    border = label;
+    return t;
+  }
+  return -1.0;
+}
+
+// the sphere as the host evaluates the ellipsoid quadratic with the
+// semi-axes r e_x, r e_y, r e_z (cross products, then the coefficients, term
+// by term in the host's order)
 __device__ __forceinline__ double sphere_crossing(const lbm_element& e, double x, double y, double z, double v0,
                                                  double v1, double v2, double dmax, int& border) {
   const double r = e.p[3];
@@ -160,103 +285,100 @@ __device__ __forceinline__ double sphere_crossing(const lbm_element& e, double x
   cross(c, a, c31);
   const double in = add(add(mul(a[0], c23[0]), mul(a[1], c23[1])), mul(a[2], c23[2]));
   const double dd = mul(in, in);
-  const double cxx = add(add(mul(c12[0], c12[0]), mul(c23[0], c23[0])), mul(c31[0], c31[0]));
-  const double cyy = add(add(mul(c12[1], c12[1]), mul(c23[1], c23[1])), mul(c31[1], c31[1]));
-  const double czz = add(add(mul(c12[2], c12[2]), mul(c23[2], c23[2])), mul(c31[2], c31[2]));
-  const double cxy = mul(2.0, add(add(mul(c12[0], c12[1]), mul(c23[0], c23[1])), mul(c31[0], c31[1])));
-  const double cyz = mul(2.0, add(add(mul(c12[1], c12[2]), mul(c23[1], c23[2])), mul(c31[1], c31[2])));
-  const double czx = mul(2.0, add(add(mul(c12[2], c12[0]), mul(c23[2], c23[0])), mul(c31[2], c31[0])));
-  const double X = sub(x, e.p[0]), Y = sub(y, e.p[1]), Z = sub(z, e.p[2]);
-  const double qa = add(add(add(add(add(mul(cxx, mul(v0, v0)), mul(cyy, mul(v1, v1))), mul(czz, mul(v2, v2))),
-                                mul(mul(cxy, v0), v1)),
-                            mul(mul(cyz, v1), v2)),
-                        mul(mul(czx, v2), v0));
-  const double bx = add(add(mul(mul(2.0, cxx), v0), mul(cxy, v1)), mul(czx, v2));
-  const double by = add(add(mul(mul(2.0, cyy), v1), mul(cyz, v2)), mul(cxy, v0));
-  const double bz = add(add(mul(mul(2.0, czz), v2), mul(czx, v0)), mul(cyz, v1));
-  const double qb = add(add(mul(bx, X), mul(by, Y)), mul(bz, Z));
-  const double qc =
-      sub(add(add(add(add(add(mul(cxx, mul(X, X)), mul(cyy, mul(Y, Y))), mul(czz, mul(Z, Z))), mul(mul(cxy, X), Y)),
-                  mul(mul(cyz, Y), Z)),
-              mul(mul(czx, Z), X)),
-          dd);
-  double disc = sub(mul(qb, qb), mul(mul(4.0, qa), qc));
-  const bool ok = disc >= 0;
-  double t1 = kFar, t2 = kFar;
-  if (ok) {
-    disc = __dsqrt_rn(disc);
-    t1 = dvd(sub(-qb, disc), mul(2.0, qa));
-    t2 = dvd(add(-qb, disc), mul(2.0, qa));
-  }
-  if (t1 < 0) t1 = kFar;
-  if (t2 < 0) t2 = kFar;
-  double t = ok ? fmin(t1, t2) : -1.0;
-  if (t == kFar) t = -1.0;
-  border = -1;
-  if (t > 0 && t <= dmax) {
-    border = e.label[0];
-    return t;
-  }
-  return -1.0;
+  double co[6];
+  co[0] = add(add(mul(c12[0], c12[0]), mul(c23[0], c23[0])), mul(c31[0], c31[0]));
+  co[1] = add(add(mul(c12[1], c12[1]), mul(c23[1], c23[1])), mul(c31[1], c31[1]));
+  co[2] = add(add(mul(c12[2], c12[2]), mul(c23[2], c23[2])), mul(c31[2], c31[2]));
+  co[3] = mul(2.0, add(add(mul(c12[0], c12[1]), mul(c23[0], c23[1])), mul(c31[0], c31[1])));
+  co[4] = mul(2.0, add(add(mul(c12[1], c12[2]), mul(c23[1], c23[2])), mul(c31[1], c31[2])));
+  co[5] = mul(2.0, add(add(mul(c12[2], c12[0]), mul(c23[2], c23[0])), mul(c31[2], c31[0])));
+  const double qa = add(add(add(add(add(mul(co[0], mul(v0, v0)), mul(co[1], mul(v1, v1))), mul(co[2], mul(v2, v2))),
+                                mul(mul(co[3], v0), v1)),
+                            mul(mul(co[4], v1), v2)),
+                        mul(mul(co[5], v2), v0));
+  const double bx = add(add(mul(mul(2.0, co[0]), v0), mul(co[3], v1)), mul(co[5], v2));
+  const double by = add(add(mul(mul(2.0, co[1]), v1), mul(co[4], v2)), mul(co[3], v0));
+  const double bz = add(add(mul(mul(2.0, co[2]), v2), mul(co[5], v0)), mul(co[4], v1));
+  return quadric_crossing(sub(x, e.p[0]), sub(y, e.p[1]), sub(z, e.p[2]), co, dd, qa, bx, by, bz, dmax, e.label[0],
+                          border);
 }
 
-__device__ __forceinline__ double crossing(const lbm_element& e, double x, double y, double vx, double vy,
+__device__ __forceinline__ double ellipsoid_crossing(const lbm_element& e, double x, double y, double z, int u,
+                                                    double dmax, int& border) {
+  const double co[6] = {e.p[3], e.p[4], e.p[5], e.p[6], e.p[7], e.p[8]};
+  return quadric_crossing(sub(x, e.p[0]), sub(y, e.p[1]), sub(z, e.p[2]), co, e.p[9], e.vq[u][0], e.vq[u][1],
+                          e.vq[u][2], e.vq[u][3], dmax, e.label[0], border);
+}
+
+// a cylinder (pylbm/elements/cylinder.py:104-216): in its frame, the side is
+// the section's boundary crossed between the caps z = -1 and z = 1, the caps
+// count where the crossing lies in the section; the first of the three wins
+// (ties: bottom, then top, then side)
+__device__ __forceinline__ double cylinder_crossing(const lbm_element& e, double x, double y, double z, int u,
+                                                   double dmax, int& border) {
+  double f[3];
+  to_frame(e, x, y, z, f);
+  const double vx = e.vq[u][0], vy = e.vq[u][1], vz = e.vq[u][2];
+  const int section = (int)e.p[12];
+  const int sides = section == 0 ? 1 : (section == 1 ? 3 : 4);
+  double alpha;
+  if (section == 0) {
+    alpha = ellipse_crossing(sub(f[0], 0.0), sub(f[1], 0.0), vx, vy, 1.0, 1.0, 0.0, 1.0, e.vq[u][3], dmax,
+                             e.label[0], border);
+  } else {
+    const double tq[3][2] = {{0, 0}, {0, 0}, {1, 0}}, tw[3][2] = {{1, 0}, {0, 1}, {-1, 1}};
+    const double sq[4][2] = {{0, 0}, {0, 0}, {1, 0}, {0, 1}}, sw[4][2] = {{1, 0}, {0, 1}, {0, 1}, {1, 0}};
+    alpha = lines_crossing(f[0], f[1], vx, vy, sides, section == 1 ? tq : sq, section == 1 ? tw : sw, e.label, dmax,
+                           border);
+  }
+  if (alpha < 0) alpha = kFar;
+  if (alpha > 0 && fabs(add(f[2], mul(alpha, vz))) > 1.0) {
+    alpha = kFar;
+    border = -1;
+  }
+  const double den = add(vz, vz == 0 ? 1.0e-16 : 0.0);
+  double top = dvd(sub(1.0, f[2]), den);
+  if (top < 0 || top > dmax || !section_inside(section, add(f[0], mul(top, vx)), add(f[1], mul(top, vy))))
+    top = kFar;
+  double bottom = dvd(-add(1.0, f[2]), den);
+  if (bottom < 0 || bottom > dmax ||
+      !section_inside(section, add(f[0], mul(bottom, vx)), add(f[1], mul(bottom, vy))))
+    bottom = kFar;
+  alpha = fmin(fmin(alpha, top), bottom);
+  if (alpha == top) border = e.label[sides + 1];
+  if (alpha == bottom) border = e.label[sides];
+  return alpha == kFar ? -1.0 : alpha;
+}
+
+__device__ __forceinline__ double crossing(const lbm_element& e, double x, double y, double vx, double vy, int u,
                                           double dmax, int& border) {
   border = -1;
   if (e.kind == LBM_ELEMENT_CIRCLE) {
     // ellipse {c + cos(a) v1 + sin(a) v2} with v1 = (r, 0), v2 = (0, r)
     const double r = e.p[2];
     const double v1x = mul(r, 1.0), v1y = mul(r, 0.0), v2x = mul(r, 0.0), v2y = mul(r, 1.0);
-    const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
     const double sxx = add(mul(v1x, v1x), mul(v2x, v2x));
     const double syy = add(mul(v1y, v1y), mul(v2y, v2y));
     const double sxy = mul(2.0, add(mul(v1x, v1y), mul(v2x, v2y)));
     const double det = sub(mul(v1x, v2y), mul(v1y, v2x));
-    const double det2 = mul(det, det);
     const double qa = sub(add(mul(mul(vx, vx), syy), mul(mul(vy, vy), sxx)), mul(mul(vx, vy), sxy));
-    const double qb = sub(add(mul(mul(mul(2.0, px), vx), syy), mul(mul(mul(2.0, py), vy), sxx)),
-                          mul(add(mul(px, vy), mul(py, vx)), sxy));
-    const double qc = sub(sub(add(mul(mul(px, px), syy), mul(mul(py, py), sxx)), mul(mul(px, py), sxy)), det2);
-    const double disc = sub(mul(qb, qb), mul(mul(4.0, qa), qc));
-    const bool ok = disc >= 0;
-    const double root = __dsqrt_rn(ok ? disc : 0.0);
-    double t1 = kFar, t2 = kFar;
-    if (qa != 0) {
-      t1 = ok ? dvd(sub(-qb, root), mul(2.0, qa)) : kFar;
-      t2 = ok ? dvd(add(-qb, root), mul(2.0, qa)) : kFar;
-    }
-    if (t1 < 0) t1 = kFar;
-    if (t2 < 0) t2 = kFar;
-    double t = ok ? fmin(t1, t2) : -1.0;
-    if (t == kFar) t = -1.0;
-    if (t > 0 && t <= dmax) {
-      border = e.label[0];
-      return t;
-    }
-    return -1.0;
+    return ellipse_crossing(sub(x, e.p[0]), sub(y, e.p[1]), vx, vy, sxx, syy, sxy, mul(det, det), qa, dmax,
+                            e.label[0], border);
+  }
+  if (e.kind == LBM_ELEMENT_ELLIPSE)
+    return ellipse_crossing(sub(x, e.p[0]), sub(y, e.p[1]), vx, vy, e.p[2], e.p[3], e.p[4], e.p[5], e.vq[u][0], dmax,
+                            e.label[0], border);
+  const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
+  if (e.kind == LBM_ELEMENT_TRIANGLE) {
+    // edges from the point along v1 and v2, then from v1 along v2 - v1
+    const double q[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {e.p[2], e.p[3]}};
+    const double w[3][2] = {{e.p[2], e.p[3]}, {e.p[4], e.p[5]}, {sub(e.p[4], e.p[2]), sub(e.p[5], e.p[3])}};
+    return lines_crossing(px, py, vx, vy, 3, q, w, e.label, dmax, border);
   }
   // parallelogram: the four edges point + s w, s in [0, 1], in the host order
-  const double px = sub(x, e.p[0]), py = sub(y, e.p[1]);
   const double q[4][2] = {{0.0, 0.0}, {0.0, 0.0}, {e.p[4], e.p[5]}, {e.p[2], e.p[3]}};
   const double w[4][2] = {{e.p[2], e.p[3]}, {e.p[4], e.p[5]}, {e.p[2], e.p[3]}, {e.p[4], e.p[5]}};
-  double alpha = kFar;
-  for (int k = 0; k < 4; ++k) {
-    const double det = sub(mul(vy, w[k][0]), mul(vx, w[k][1]));
-    if (det == 0) continue;
-    const double inv = dvd(1.0, det);
-    const double c1 = sub(q[k][0], px), c2 = sub(q[k][1], py);
-    const double t = mul(add(mul(-w[k][1], c1), mul(w[k][0], c2)), inv);
-    const double s = mul(add(mul(-vy, c1), mul(vx, c2)), inv);
-    if (t > 0 && s >= 0 && s <= 1 && t <= dmax && alpha > t) {
-      alpha = t;
-      border = e.label[k];
-    }
-  }
-  if (alpha == kFar) {
-    border = -1;
-    return -1.0;
-  }
-  return alpha;
+  return lines_crossing(px, py, vx, vy, 4, q, w, e.label, dmax, border);
 }
 
 __device__ __forceinline__ long long box_offset(const Box& b, const int (&i)[3]) {
@@ -290,11 +412,16 @@ __global__ void k_element_links(Box b, lbm_domain d, Region r, lbm_element e, co
   int j[3] = {i[0] + vx, i[1] + vy, i[2] + vz};
   const bool out = ioo[box_offset(b, j)] == kValOut;
   int border;
-  const double alpha =
-      e.kind == LBM_ELEMENT_SPHERE
-          ? sphere_crossing(e, x, y, z, mul(d.dx, (double)vx), mul(d.dx, (double)vy), mul(d.dx, (double)vz), 1.0,
-                            border)
-          : crossing(e, x, y, mul(d.dx, (double)vx), mul(d.dx, (double)vy), 1.0, border);
+  double alpha;
+  if (e.kind == LBM_ELEMENT_SPHERE)
+    alpha = sphere_crossing(e, x, y, z, mul(d.dx, (double)vx), mul(d.dx, (double)vy), mul(d.dx, (double)vz), 1.0,
+                            border);
+  else if (e.kind == LBM_ELEMENT_ELLIPSOID)
+    alpha = ellipsoid_crossing(e, x, y, z, u, 1.0, border);
+  else if (e.kind == LBM_ELEMENT_CYLINDER)
+    alpha = cylinder_crossing(e, x, y, z, u, 1.0, border);
+  else
+    alpha = crossing(e, x, y, mul(d.dx, (double)vx), mul(d.dx, (double)vy), u, 1.0, border);
   const bool sel = alpha > 0 && !solid && out;
   double dk = dist[(long long)u * b.nodes + o];
   int fk = flag[(long long)u * b.nodes + o];
@@ -408,9 +535,13 @@ int lbm_domain_element(const lbm_domain* d, const lbm_element* e, const double* 
   int rc = check_domain(d, "lbm_domain_element");
   if (rc) return rc;
   if (!e || !coords || !in_or_out || !distance || !flag) return fail(LBM_ERR_ARG, "lbm_domain_element: NULL argument");
-  if (e->kind != LBM_ELEMENT_CIRCLE && e->kind != LBM_ELEMENT_PARALLELOGRAM && e->kind != LBM_ELEMENT_SPHERE)
+  if (e->kind < LBM_ELEMENT_CIRCLE || e->kind > LBM_ELEMENT_CYLINDER)
     return fail(LBM_ERR_ARG, "lbm_domain_element: kind %d", e->kind);
-  if (d->dim != (e->kind == LBM_ELEMENT_SPHERE ? 3 : 2))
+  if (e->kind == LBM_ELEMENT_CYLINDER && (e->p[12] < 0 || e->p[12] > 2))
+    return fail(LBM_ERR_ARG, "lbm_domain_element: cylinder section %g", e->p[12]);
+  const bool solid3d =
+      e->kind == LBM_ELEMENT_SPHERE || e->kind == LBM_ELEMENT_ELLIPSOID || e->kind == LBM_ELEMENT_CYLINDER;
+  if (d->dim != (solid3d ? 3 : 2))
     return fail(LBM_ERR_UNSUPPORTED, "lbm_domain_element: element kind %d on a %dD domain", e->kind, d->dim);
   Region r;
   r.nodes = 1;

@@ -229,11 +229,19 @@ class Domain:
         elif isinstance(elem, geometry.Sphere):
             e.kind = runtime.LBM_ELEMENT_SPHERE
             vals = [*elem.center, elem.radius]
+        elif hasattr(elem, "device_params") and isinstance(elem, geometry.Element):
+            kinds = {geometry.Ellipse: runtime.LBM_ELEMENT_ELLIPSE, geometry.Triangle: runtime.LBM_ELEMENT_TRIANGLE,
+                     geometry.Ellipsoid: runtime.LBM_ELEMENT_ELLIPSOID}
+            e.kind = kinds.get(type(elem), runtime.LBM_ELEMENT_CYLINDER)
+            vals, labels, table = elem.device_params(self.dx, self.stencil.unique_v)
+            for u, row in enumerate(table):
+                for i, v in enumerate(row):
+                    e.vq[u][i] = float(v)
         else:
             raise NotImplementedError(f"{type(elem).__name__} is not built on the device")
         for i, v in enumerate(vals):
             e.p[i] = float(v)
-        for i, lab in enumerate(elem.label[:4]):
+        for i, lab in enumerate(elem.label[:6]):
             e.label[i] = int(lab)
         e.isfluid = int(elem.isfluid)
         nmin, nmax = self._region(elem)

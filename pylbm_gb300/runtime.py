@@ -61,6 +61,10 @@ LBM_INSTANCE_PAIRS = 1
 LBM_ELEMENT_CIRCLE = 1
 LBM_ELEMENT_PARALLELOGRAM = 2
 LBM_ELEMENT_SPHERE = 3
+LBM_ELEMENT_ELLIPSE = 4
+LBM_ELEMENT_TRIANGLE = 5
+LBM_ELEMENT_ELLIPSOID = 6
+LBM_ELEMENT_CYLINDER = 7
 
 
 class DomainDesc(ctypes.Structure):
@@ -101,10 +105,11 @@ class ElementDesc(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int32),
         ("isfluid", ctypes.c_int32),
-        ("label", ctypes.c_int32 * 4),
-        ("p", ctypes.c_double * 8),
+        ("label", ctypes.c_int32 * 6),
+        ("p", ctypes.c_double * 24),
         ("lo", ctypes.c_int32 * 3),
         ("hi", ctypes.c_int32 * 3),
+        ("vq", (ctypes.c_double * 4) * LBM_MAX_Q),
     ]
 
 

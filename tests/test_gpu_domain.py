@@ -8,10 +8,14 @@ import numpy as np
 import pytest
 
 import demo_cases
+import element_cases
+from conftest import golden
+from pylbm_gb300 import geometry
 from pylbm_gb300 import workloads as W
 from pylbm_gb300.boundary import Boundary
 from pylbm_gb300.domain import Domain
 from pylbm_gb300.scheme import Scheme
+from test_elements import assert_domain_equals_fixture
 
 pytestmark = pytest.mark.gpu
 
@@ -55,6 +59,23 @@ def test_device_domain_equals_host(name):
         assert np.array_equal(mh.istore, md.istore)
         assert np.array_equal(mh.ilabel, md.ilabel)
         assert np.array_equal(mh.distance.view(np.int64), md.distance.view(np.int64))
+
+
+@pytest.mark.parametrize("name", list(element_cases.cases(geometry)))
+def test_device_elements_equal_host_and_reference(name):
+    """Ellipse, triangle, ellipsoid and the four cylinders built on the device:
+    the same arrays as the host build, bit for bit, and as the reference's
+    own Domain (tests/golden/elements.npz; distances to 1e-13 relative, the
+    fixture's host libraries may round a tilted frame differently)."""
+    d = element_cases.cases(geometry)[name]
+    host = Domain(d)
+    dev = Domain(d, device=True)
+    ioo, dist, flag = dev.download_arrays()
+    assert np.array_equal(ioo, host.in_or_out)
+    assert np.array_equal(flag, host.flag)
+    assert np.array_equal(dist.view(np.int64), host.distance.view(np.int64))
+    host.in_or_out, host.distance, host.flag = ioo, dist, flag
+    assert_domain_equals_fixture(host, name, golden("elements.npz"), rtol=1e-13)
 
 
 def test_large_disc_domain_on_device():
