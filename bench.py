@@ -413,7 +413,8 @@ def main():
     launches_per_step = sim.launches_per_step()
     step_kernel = ("lbm_scheme::k_step_periodic_closure" + ("_tc" if sim._closure_on_tensor_cores() else "")
                    if args.workload == "closure"
-                   else "lbm_scheme::k_step_walls" if sim._folded()
+                   else "lbm_scheme::k_step_walls" + ("_pairs" if args.dtype in ("float16", "bfloat16") else "")
+                   if sim._folded()
                    else "lbm_scheme::k_step_periodic_pairs" if sim.periodic and args.dtype in ("float16", "bfloat16")
                    else "lbm_scheme::k_step_periodic" if sim.periodic else "lbm_scheme::k_step_ghost")
     for _ in range(args.warmup):

@@ -225,10 +225,10 @@ class Simulation:
         self._batch_rhs = []        # (device array, method index, host builder) of batch right-hand sides that follow time_bc
         self._full_halo = True
         self.batch_boundary = True  # one launch for all boundary methods where the lists allow it
-        # bounce-back box walls applied in the pull where the links allow it;
-        # with 16-bit storage the boundary launch plus the two-node ghost step
-        # measured faster (cube 256^3: 0.264 against 0.286 ms per step)
-        self.fold_walls = dtype in ("float64", "float32")
+        # bounce-back box walls applied in the pull where the links allow it
+        # (cube 256^3 per step: FP32 0.396 against 0.430 ms with the boundary
+        # launch, FP16 0.249 against 0.256, BF16 0.250 against 0.253)
+        self.fold_walls = True
         self._walls = None          # (constants nv x 27, opposite populations) of lbm_one_time_step_walls
         self._graph = None
         self._graph_key = None

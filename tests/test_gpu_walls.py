@@ -24,7 +24,7 @@ def test_folded_walls_equal_boundary_launch(case, dtype):
     for fold in (True, False):
         sim = Simulation(make(), dtype=dtype)
         assert sim._walls is not None
-        assert sim.fold_walls == (dtype in ("float64", "float32"))  # the default
+        assert sim.fold_walls  # the default
         sim.fold_walls = fold
         assert sim.launches_per_step() == (1 if fold else 2)
         sim.run(25)
