@@ -402,6 +402,14 @@ int lbm_mlp_tc_timeouts(uint32_t* count);
  * loss to *loss (device).  scratch: lbm_mlp_scratch_bytes(n) bytes. */
 int lbm_mlp_gradients(const void* x, const float* target, int32_t n, const void* wbf16, const float* params,
                       float* grad, float* loss, void* scratch, size_t scratch_bytes, void* stream);
+/* The same gradients and loss from one kernel on the 5th-generation tensor
+ * cores: per 128-sample tile the forward pass, the loss, the backward pass
+ * and the weight gradients run in shared and tensor memory (no scratch; the
+ * gradients accumulate in tensor memory over a block's tiles and reach grad
+ * once per block).  Any n > 0; the rounding points of lbm_mlp_gradients, the
+ * FP32 accumulation order differs.  Bounded waits as lbm_mlp_forward_tc. */
+int lbm_mlp_gradients_tc(const void* x, const float* target, int32_t n, const float* params, float* grad, float* loss,
+                         void* stream);
 /* Adam update of params (moments m, v), zeroes grad, refreshes wbf16. */
 int lbm_mlp_adam(float* params, float* m, float* v, float* grad, float lr, float beta1, float beta2, float eps,
                  int32_t step, void* wbf16, void* stream);

@@ -62,6 +62,9 @@ class Mlp:
             b.zero(stream)
         self.step = 0
         self._scratch = None
+        # "tc": k_mlp_train_tc (tcgen05, one kernel; 26.6 us per Adam step of
+        # 2048 samples); "warp": k_mlp_fwd_bwd + k_mlp_wgrad (mma.sync, 279 us)
+        self.train_kernel = "tc"
         self.sync()
 
     def sync(self):
@@ -118,7 +121,7 @@ class Mlp:
     def _device_data(self, x, t):
         xb = _bf16_bits(x)
         n = xb.shape[0]
-        if n % 16:
+        if n % 16 and self.train_kernel == "warp":
             raise ValueError("the batch size must be a multiple of 16")
         dx = runtime.DeviceBuffer(xb.nbytes)
         dx.upload(xb, stream=self.stream)
@@ -144,11 +147,19 @@ class Mlp:
 
     # ---------------------------------------------------------- device arrays
     def gradients_device(self, dx, dt, n, read_loss=True):
-        scratch = self._scratch_for(n)
-        runtime.check(self._core.lbm_mlp_gradients(dx.handle if hasattr(dx, "handle") else dx,
-                                                   dt.handle if hasattr(dt, "handle") else dt, n, self.w.handle,
-                                                   self.p.handle, self.g.handle, self.loss.handle, scratch.handle,
-                                                   scratch.nbytes, self.stream))
+        xh = dx.handle if hasattr(dx, "handle") else dx
+        th = dt.handle if hasattr(dt, "handle") else dt
+        if self.train_kernel == "tc":
+            # forward, backward and weight gradients of 128-sample tiles in one
+            # tcgen05 kernel, nothing staged in global memory
+            runtime.check(self._core.lbm_mlp_gradients_tc(xh, th, n, self.p.handle, self.g.handle, self.loss.handle,
+                                                          self.stream))
+        elif self.train_kernel == "warp":
+            scratch = self._scratch_for(n)
+            runtime.check(self._core.lbm_mlp_gradients(xh, th, n, self.w.handle, self.p.handle, self.g.handle,
+                                                       self.loss.handle, scratch.handle, scratch.nbytes, self.stream))
+        else:
+            raise ValueError(f"train_kernel: {self.train_kernel!r} (tc or warp)")
         if not read_loss:
             return None
         out = np.empty(1, dtype=np.float32)

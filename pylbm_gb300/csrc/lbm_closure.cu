@@ -418,6 +418,34 @@ int lbm_mlp_forward_tc(const void* x, int32_t n, const float* params, float* y, 
   return launch_check("lbm_mlp_forward_tc");
 }
 
+int lbm_mlp_gradients_tc(const void* x, const float* target, int32_t n, const float* params, float* grad, float* loss,
+                         void* stream) {
+  if (!x || !target || !params || !grad || !loss) return fail(LBM_ERR_ARG, "lbm_mlp_gradients_tc: NULL");
+  if (n <= 0) return fail(LBM_ERR_ARG, "lbm_mlp_gradients_tc: n=%d", n);
+  const char* who = "lbm_mlp_gradients_tc";
+  int dev = 0, sms = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), who);
+  if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), who);
+  if (rc) return rc;
+  static bool sized[64];  // dynamic shared memory above 48 KB, allowed once per device
+  if (dev < 0 || dev >= 64 || !sized[dev]) {
+    rc = cuda_check(cudaFuncSetAttribute(lbm_mlp_tc::k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         lbm_mlp_tc::train::kSmem),
+                    who);
+    if (rc) return rc;
+    if (dev >= 0 && dev < 64) sized[dev] = true;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = cuda_check(cudaMemsetAsync(loss, 0, sizeof(float), st), who);
+  if (rc) return rc;
+  // one block per SM: each holds all 512 tensor-memory columns
+  const int tiles = (n + lbm_mlp_tc::kRows - 1) / lbm_mlp_tc::kRows;
+  const int blocks = tiles < sms ? tiles : sms;
+  lbm_mlp_tc::k_mlp_train_tc<<<blocks, lbm_mlp_tc::kThreads, lbm_mlp_tc::train::kSmem, st>>>(
+      (const __nv_bfloat16*)x, target, n, params, grad, loss);
+  return launch_check(who);
+}
+
 int lbm_mlp_tc_timeouts(uint32_t* count) {
   if (!count) return fail(LBM_ERR_ARG, "lbm_mlp_tc_timeouts: NULL");
   return cuda_check(cudaMemcpyFromSymbol(count, lbm_mlp_tc::mlp_tc_timeouts, sizeof(uint32_t)),

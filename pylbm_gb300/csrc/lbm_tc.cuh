@@ -29,6 +29,21 @@ __host__ __device__ constexpr uint32_t instr_desc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// the same with A and/or B MN-major (bits 15 / 16: the operand's M or N index
+// is the contiguous one).  The MN-major no-swizzle layout: core matrices of
+// 8 K-rows x 8 MN-elements (16-byte rows), the stride byte offset steps
+// between core matrices along MN, the leading byte offset between groups of
+// 8 along K.
+__host__ __device__ constexpr uint32_t instr_desc_mn(int m, int n, bool a_mn, bool b_mn) {
+  return instr_desc(m, n) | (a_mn ? 1u << 15 : 0u) | (b_mn ? 1u << 16 : 0u);
+}
+
+// byte offset of element (r, k) of a K-major operand whose 8-row groups are
+// group_bytes apart (core_offset is the dense case, group_bytes = K / 8 * 128)
+__device__ __forceinline__ uint32_t group_offset(int r, int k, int group_bytes) {
+  return (uint32_t)((r >> 3) * group_bytes + ((k >> 3) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+}
+
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(
@@ -132,7 +147,7 @@ __device__ __forceinline__ void stage_bf16(unsigned char* dst, const float* __re
 // into row `row` of the next layer's [..][N] K-major A operand
 template <int N, class Act>
 __device__ __forceinline__ void epilogue_bf16(uint32_t taddr, const float* bias, unsigned char* dst, int row,
-                                              Act act) {
+                                              int group_bytes, Act act) {
 #pragma unroll
   for (int c = 0; c < N; c += 32) {
     float v[32];
@@ -140,8 +155,22 @@ __device__ __forceinline__ void epilogue_bf16(uint32_t taddr, const float* bias,
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = act(v[j] + bias[c + j]);
 #pragma unroll
-    for (int j = 0; j < 32; j += 8) store8_bf16(dst, core_offset(row, c + j, N), v + j);
+    for (int j = 0; j < 32; j += 8) store8_bf16(dst, group_offset(row, c + j, group_bytes), v + j);
   }
+}
+
+template <int N, class Act>
+__device__ __forceinline__ void epilogue_bf16(uint32_t taddr, const float* bias, unsigned char* dst, int row,
+                                              Act act) {
+  epilogue_bf16<N>(taddr, bias, dst, row, N / 8 * 128, act);
+}
+
+// the block's generic-proxy shared-memory writes made visible to the tensor
+// cores, and its tensor-memory reads ordered, before one thread issues MMAs
+__device__ __forceinline__ void sync_for_mma() {
+  fence_async_smem();
+  fence_before_sync();
+  __syncthreads();
 }
 
 // wait for the block's MMA commit of the current phase; false when any thread

@@ -51,9 +51,14 @@ def test_tensor_memory_forward_matches_oracle_and_warp_forward(n):
     assert count.value == 0
 
 
-@pytest.mark.parametrize("n", [16, 4096, 10000 - 10000 % 16])
-def test_gradients_match_oracle(n):
+@pytest.mark.parametrize("kernel,n", [("warp", 16), ("warp", 4096), ("warp", 10000 - 10000 % 16),
+                                      ("tc", 16), ("tc", 1000), ("tc", 4096), ("tc", 40000)])
+def test_gradients_match_oracle(kernel, n):
+    """warp: k_mlp_fwd_bwd + k_mlp_wgrad; tc: k_mlp_train_tc (tcgen05, one
+    kernel, gradients accumulated in tensor memory; any n, partial last
+    tile, several tiles per block at n = 40000)."""
     mlp = Mlp(seed=5)
+    mlp.train_kernel = kernel
     x, t = _data(n, seed=n)
     loss, grad = mlp.gradients(x, t)
     p = mlp.params_host().astype(np.float64)
@@ -72,9 +77,29 @@ def test_gradients_match_oracle(n):
         if np.linalg.norm(ref[blk]) > 0:
             assert np.linalg.norm(grad[blk] - ref[blk]) / np.linalg.norm(ref[blk]) < 2e-2, name
         i += k
+    if kernel == "tc":
+        count = ctypes.c_uint32()
+        runtime.check(runtime.core().lbm_mlp_tc_timeouts(ctypes.byref(count)))
+        assert count.value == 0
 
 
-def test_adam_training_reduces_loss():
+def test_tensor_core_gradients_equal_warp_gradients():
+    """The two training paths on the same batch: the same loss and gradients
+    up to the FP32 accumulation order (a BF16 activation or gradient may round
+    to its neighbour)."""
+    x, t = _data(4096, seed=11)
+    out = {}
+    for kernel in ("warp", "tc"):
+        mlp = Mlp(seed=9)
+        mlp.train_kernel = kernel
+        out[kernel] = mlp.gradients(x, t)
+    (lw, gw), (lt, gt) = out["warp"], out["tc"]
+    assert abs(lw - lt) <= 1e-5 * lw
+    assert np.linalg.norm(gt - gw) / np.linalg.norm(gw) < 5e-3
+
+
+@pytest.mark.parametrize("kernel", ["warp", "tc"])
+def test_adam_training_reduces_loss(kernel):
     """Fit a smooth map with the GPU training step; the loss must drop."""
     rng = np.random.default_rng(7)
     n = 8192
@@ -84,6 +109,7 @@ def test_adam_training_reduces_loss():
     t = np.zeros((n, mo.OUT))
     t[:, :6] = np.tanh(x[:, :6] * 0.7) + 0.3 * x[:, 1:7] * x[:, 2:8]
     mlp = Mlp(seed=11)
+    mlp.train_kernel = kernel
     first = mlp.train_step(x, t, lr=3e-3)
     for _ in range(300):
         last = mlp.train_step(x, t, lr=3e-3)
