@@ -410,6 +410,16 @@ int lbm_mlp_gradients(const void* x, const float* target, int32_t n, const void*
  * FP32 accumulation order differs.  Bounded waits as lbm_mlp_forward_tc. */
 int lbm_mlp_gradients_tc(const void* x, const float* target, int32_t n, const float* params, float* grad, float* loss,
                          void* stream);
+/* Vector-Jacobian product of the MLP on the same tensor-core kernel: adds
+ * sum over samples of dy . dy_out/dparams to grad, for dy (n x 8 FP32, the
+ * first 6 columns used) the gradient of some loss with respect to the
+ * outputs lbm_mlp_forward_tc returns; *dot (device) receives sum dy . y.
+ * This is the backward step of an MLP that sits inside a differentiated
+ * computation (a training loss over several closure time steps); no
+ * counterpart in pylbm, which has no learned closure (its relaxation is
+ * pylbm/algorithm/base.py:404-428). */
+int lbm_mlp_vjp_tc(const void* x, const float* dy, int32_t n, const float* params, float* grad, float* dot,
+                   void* stream);
 /* Adam update of params (moments m, v), zeroes grad, refreshes wbf16. */
 int lbm_mlp_adam(float* params, float* m, float* v, float* grad, float lr, float beta1, float beta2, float eps,
                  int32_t step, void* wbf16, void* stream);

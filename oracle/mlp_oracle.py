@@ -1,7 +1,8 @@
 """CPU oracle of the learned-closure MLP (float64 NumPy).
 
 TEST INFRASTRUCTURE ONLY: checks the GPU forward pass and gradients of
-pylbm_gb300's MLP kernels (lbm_mlp_forward / lbm_mlp_gradients).
+pylbm_gb300's MLP kernels (lbm_mlp_forward / lbm_mlp_gradients /
+lbm_mlp_vjp_tc).
 
 Network x(16) -> 64 SiLU -> 64 SiLU -> y(8); loss = mean over samples and the
 first 6 outputs of (y - target)^2.  Parameters use the FP32 block layout of
@@ -71,19 +72,35 @@ def forward(p, x, bf16_points=True):
     return y, (x, z1, h1, z2, h2, W1, W2, W3)
 
 
-def loss_and_grad(p, x, target, bf16_points=True):
-    r = bf16 if bf16_points else (lambda v: np.asarray(v, dtype=np.float64))
-    n = x.shape[0]
-    y, (xr, z1, h1, z2, h2, W1, W2, W3) = forward(p, x, bf16_points)
-    diff = np.zeros_like(y)
-    diff[:, :NUSED] = y[:, :NUSED] - target[:, :NUSED]
-    loss = float((diff ** 2).sum() / (NUSED * n))
-    dy = r(2.0 * diff / (NUSED * n))
+def _backward(dy, cache, r):
+    xr, z1, h1, z2, h2, W1, W2, W3 = cache
+    dy = r(dy)
     dh2 = r((dy @ W3) * _silu_grad(z2))
     dh1 = r((dh2 @ W2) * _silu_grad(z1))
     g = {"W3": dy.T @ h2, "b3": dy.sum(0), "W2": dh2.T @ h1, "b2": dh2.sum(0), "W1": dh1.T @ xr,
          "b1": dh1.sum(0)}
-    return loss, pack(g)
+    return pack(g)
+
+
+def loss_and_grad(p, x, target, bf16_points=True):
+    r = bf16 if bf16_points else (lambda v: np.asarray(v, dtype=np.float64))
+    n = x.shape[0]
+    y, cache = forward(p, x, bf16_points)
+    diff = np.zeros_like(y)
+    diff[:, :NUSED] = y[:, :NUSED] - target[:, :NUSED]
+    loss = float((diff ** 2).sum() / (NUSED * n))
+    return loss, _backward(2.0 * diff / (NUSED * n), cache, r)
+
+
+def vjp(p, x, dy, bf16_points=True):
+    """(sum of dy . y, gradient of that sum) over the first 6 outputs: the
+    backward step of the MLP inside a larger differentiated computation, dy
+    being the loss gradient with respect to the outputs."""
+    r = bf16 if bf16_points else (lambda v: np.asarray(v, dtype=np.float64))
+    y, cache = forward(p, x, bf16_points)
+    d = np.zeros_like(y)
+    d[:, :NUSED] = np.asarray(dy, dtype=np.float64)[:, :NUSED]
+    return float((d * y).sum()), _backward(d, cache, r)
 
 
 def finite_difference(p, x, target, idx, eps=1e-6):

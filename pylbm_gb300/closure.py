@@ -118,6 +118,43 @@ class Mlp:
         dy.free()
         return y.astype(np.float64)
 
+    def forward_device(self, x, n, y):
+        """lbm_mlp_forward_tc on device pointers: x (n, 16) BF16 rows, y (n, 8) FP32."""
+        runtime.check(self._core.lbm_mlp_forward_tc(ctypes.c_void_p(x), n, self.p.handle, ctypes.c_void_p(y),
+                                                    self.stream))
+
+    def vjp_device(self, x, dy, n):
+        """Adds the gradient of sum(dy . y) over the 6 used outputs to the
+        gradient buffer (lbm_mlp_vjp_tc; device pointers, dy (n, 8) FP32)."""
+        runtime.check(self._core.lbm_mlp_vjp_tc(ctypes.c_void_p(x), ctypes.c_void_p(dy), n, self.p.handle,
+                                                self.g.handle, self.loss.handle, self.stream))
+
+    def vjp(self, x, dy):
+        """(sum of dy . y, gradient float64) for host arrays x (n, 16), dy (n, 8)."""
+        dx, ddy, n = self._device_data(x, dy)
+        self.g.zero(self.stream)
+        self.vjp_device(dx.ptr, ddy.ptr, n)
+        grad = np.empty(self.nparam, dtype=np.float32)
+        self.g.download(grad, stream=self.stream)
+        self.g.zero(self.stream)
+        dot = np.empty(1, dtype=np.float32)
+        self.loss.download(dot, stream=self.stream)
+        return float(dot[0]), grad.astype(np.float64)
+
+    def grad_host(self):
+        out = np.empty(self.nparam, dtype=np.float32)
+        self.g.download(out, stream=self.stream)
+        return out
+
+    def set_grad(self, g):
+        self.g.upload(np.asarray(g, dtype=np.float32), stream=self.stream)
+
+    def adam_step(self, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+        """Adam update from the accumulated gradient (which it zeroes)."""
+        self.step += 1
+        runtime.check(self._core.lbm_mlp_adam(self.p.handle, self.m.handle, self.v.handle, self.g.handle, lr, beta1,
+                                              beta2, eps, self.step, self.w.handle, self.stream))
+
     def _device_data(self, x, t):
         xb = _bf16_bits(x)
         n = xb.shape[0]

@@ -418,11 +418,10 @@ int lbm_mlp_forward_tc(const void* x, int32_t n, const float* params, float* y, 
   return launch_check("lbm_mlp_forward_tc");
 }
 
-int lbm_mlp_gradients_tc(const void* x, const float* target, int32_t n, const float* params, float* grad, float* loss,
-                         void* stream) {
-  if (!x || !target || !params || !grad || !loss) return fail(LBM_ERR_ARG, "lbm_mlp_gradients_tc: NULL");
-  if (n <= 0) return fail(LBM_ERR_ARG, "lbm_mlp_gradients_tc: n=%d", n);
-  const char* who = "lbm_mlp_gradients_tc";
+static int train_tc(const void* x, const float* target, int32_t n, const float* params, float* grad, float* loss,
+                    void* stream, bool upstream, const char* who) {
+  if (!x || !target || !params || !grad || !loss) return fail(LBM_ERR_ARG, "%s: NULL", who);
+  if (n <= 0) return fail(LBM_ERR_ARG, "%s: n=%d", who, n);
   int dev = 0, sms = 0;
   int rc = cuda_check(cudaGetDevice(&dev), who);
   if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), who);
@@ -442,8 +441,18 @@ int lbm_mlp_gradients_tc(const void* x, const float* target, int32_t n, const fl
   const int tiles = (n + lbm_mlp_tc::kRows - 1) / lbm_mlp_tc::kRows;
   const int blocks = tiles < sms ? tiles : sms;
   lbm_mlp_tc::k_mlp_train_tc<<<blocks, lbm_mlp_tc::kThreads, lbm_mlp_tc::train::kSmem, st>>>(
-      (const __nv_bfloat16*)x, target, n, params, grad, loss);
+      (const __nv_bfloat16*)x, target, n, params, grad, loss, upstream);
   return launch_check(who);
+}
+
+int lbm_mlp_gradients_tc(const void* x, const float* target, int32_t n, const float* params, float* grad, float* loss,
+                         void* stream) {
+  return train_tc(x, target, n, params, grad, loss, stream, false, "lbm_mlp_gradients_tc");
+}
+
+int lbm_mlp_vjp_tc(const void* x, const float* dy, int32_t n, const float* params, float* grad, float* dot,
+                   void* stream) {
+  return train_tc(x, dy, n, params, grad, dot, stream, true, "lbm_mlp_vjp_tc");
 }
 
 int lbm_mlp_tc_timeouts(uint32_t* count) {

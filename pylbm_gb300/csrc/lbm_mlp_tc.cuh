@@ -228,7 +228,8 @@ __device__ __forceinline__ void backward_epilogue(uint32_t t_acc, uint32_t t_z, 
 __global__ void __launch_bounds__(kThreads, 1) k_mlp_train_tc(const __nv_bfloat16* __restrict__ x,
                                                               const float* __restrict__ target, int n,
                                                               const float* __restrict__ params,
-                                                              float* __restrict__ grad, float* __restrict__ loss) {
+                                                              float* __restrict__ grad, float* __restrict__ loss,
+                                                              bool upstream) {
   using namespace train;
   extern __shared__ __align__(1024) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -343,9 +344,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train_tc(const __nv_bfloat1
       for (int j = 0; j < 16; ++j) d[j] = 0.0f;
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
-        const float diff = active ? y[j] + b3[j] - tg[j] : 0.0f;
-        my_loss += diff * diff;
-        d[j] = scale * diff;
+        if (upstream) {  // target holds dLoss/dy: the pass is a vector-Jacobian product
+          const float g = active ? tg[j] : 0.0f;
+          my_loss += g * (y[j] + b3[j]);
+          d[j] = g;
+        } else {
+          const float diff = active ? y[j] + b3[j] - tg[j] : 0.0f;
+          my_loss += diff * diff;
+          d[j] = scale * diff;
+        }
       }
       store8_bf16(Q, group_offset(tid, 64, kQGroup), d);
       store8_bf16(Q, group_offset(tid, 72, kQGroup), d + 8);
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train_tc(const __nv_bfloat1
     first = false;
   }
   for (int o = 16; o > 0; o >>= 1) my_loss += __shfl_xor_sync(0xffffffffu, my_loss, o);
-  if (ok && lane == 0) atomicAdd(loss, my_loss / (6.0f * (float)n));
+  if (ok && lane == 0) atomicAdd(loss, upstream ? my_loss : my_loss / (6.0f * (float)n));
   if (ok) {
     // row tid of the accumulated gradients (columns per the buffers' features)
     if (warp < 2) {  // rows 0..63: dW1 (columns 0..15), b1 (80), dW3^T (D2 columns 0..7)

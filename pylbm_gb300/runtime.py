@@ -254,6 +254,7 @@ def core():
             _sig(lib, "lbm_mlp_forward_tc", I32, [P, I32, P, P, P])
             _sig(lib, "lbm_mlp_tc_timeouts", I32, [ctypes.POINTER(ctypes.c_uint32)])
             _sig(lib, "lbm_mlp_gradients_tc", I32, [P, P, I32, P, P, P, P])
+            _sig(lib, "lbm_mlp_vjp_tc", I32, [P, P, I32, P, P, P, P])
             _sig(lib, "lbm_mlp_gradients", I32, [P, P, I32, P, P, P, P, P, SZ, P])
             _sig(lib, "lbm_mlp_adam", I32, [P, P, P, P, F32, F32, F32, F32, I32, P, P])
             _core = lib

@@ -1,0 +1,48 @@
+"""The PyTorch restatement of the coarse step used by the a-posteriori
+closure training (pylbm_gb300/closure_train.py) against the oracle's step."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import OracleSimulation
+from pylbm_gb300.closure import study_dicos
+from pylbm_gb300.closure_train import CoarseStep, vorticity
+from pylbm_gb300.closure import vorticity as np_vorticity
+
+
+def _interior(o):
+    h = o.h
+    return o.f[:, h[0]:h[0] + o.n[0], h[1]:h[1] + o.n[1]].copy()
+
+
+@pytest.mark.parametrize("seed", [0, 7])
+def test_coarse_step_matches_oracle_float64(seed):
+    o = OracleSimulation(study_dicos(seed, 32, re=3000.0))
+    o.initialize()
+    step = CoarseStep(o.scheme, dtype=torch.float64)
+    f = torch.tensor(_interior(o))[None]
+    for _ in range(6):
+        f = step(f)
+        o.one_time_step()
+    ref = _interior(o)
+    assert np.abs(f[0].numpy() - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_coarse_step_closure_adds_to_non_conserved_moments_only():
+    o = OracleSimulation(study_dicos(1, 16, re=3000.0))
+    o.initialize()
+    step = CoarseStep(o.scheme, dtype=torch.float64)
+    f = torch.tensor(_interior(o))[None]
+    corr = torch.full((1, 6, 16, 16), 1e-3, dtype=torch.float64)
+    a = step.moments(step(f))
+    b = step.moments(step(f, lambda m: corr))
+    assert torch.allclose(a[:, :3], b[:, :3], rtol=0, atol=1e-15)
+    assert torch.allclose(b[:, 3:] - a[:, 3:], corr, rtol=0, atol=1e-14)
+
+
+def test_vorticity_matches_numpy():
+    rng = np.random.default_rng(0)
+    cons = rng.normal(size=(3, 12, 10))
+    cons[0] += 3.0
+    got = vorticity(torch.tensor(cons)[None])[0].numpy()
+    assert np.allclose(got, np_vorticity(cons[1:], cons[0]), rtol=1e-14, atol=1e-14)

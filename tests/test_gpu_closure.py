@@ -114,3 +114,23 @@ def test_adam_training_reduces_loss(kernel):
     for _ in range(300):
         last = mlp.train_step(x, t, lr=3e-3)
     assert last < 0.2 * first, (first, last)
+
+
+@pytest.mark.parametrize("n", [16, 1000, 40000])
+def test_vector_jacobian_product_matches_oracle(n):
+    """lbm_mlp_vjp_tc: the gradient of sum(dy . y) for a given output
+    gradient dy (the backward step of the a-posteriori training), against
+    the oracle with the same BF16 rounding points and the exact float64 one."""
+    mlp = Mlp(seed=4)
+    x, dy = _data(n, seed=n + 1)
+    dot, grad = mlp.vjp(x, dy)
+    p = mlp.params_host().astype(np.float64)
+    ref_dot, ref = mo.vjp(p, x, dy, bf16_points=True)
+    _, exact = mo.vjp(p, x, dy, bf16_points=False)
+    y_ref, _ = mo.forward(p, x)
+    assert abs(dot - ref_dot) <= 5e-3 * np.abs(dy[:, :6] * y_ref[:, :6]).sum()
+    assert np.linalg.norm(grad - ref) / np.linalg.norm(ref) < 5e-3
+    assert np.linalg.norm(grad - exact) / np.linalg.norm(exact) < 5e-2
+    count = ctypes.c_uint32()
+    runtime.check(runtime.core().lbm_mlp_tc_timeouts(ctypes.byref(count)))
+    assert count.value == 0
