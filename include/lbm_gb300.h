@@ -493,20 +493,28 @@ int lbm_scheme_wait_timeouts(uint32_t* count);
  * whose corrections are not all finite and within guard[0] * (the largest
  * change the relaxation made to its non-conserved moments) + guard[1] keeps
  * the plain MRT collision (bit for bit that of lbm_one_time_step_periodic)
- * and adds one to *fallbacks (device int32, or NULL).  grid > 0 caps the
- * number of blocks (persistent loop).  Needs nv <= 16 and nv - nconsm <= 8. */
+ * and adds one to *fallbacks (device int32, or NULL).  rate (host, 16
+ * floats, or NULL for the additive form above): the rate form, lo[8] then
+ * hi[8] with -1 <= lo <= hi; output j then scales the relaxation's own
+ * change of moment j, corr_j = lam_j * (m_relaxed_j - m_j) with
+ * lam_j = lo[j] + (hi[j] - lo[j]) * sigmoid(y_j * sig_out[j] + mu_out[j]),
+ * i.e. the node relaxes moment j at the rate s_j * (1 + lam_j), inside
+ * bounds the caller chooses (effective rates below 2 keep the collision
+ * stable).  grid > 0 caps the number of blocks (persistent loop).  Needs
+ * nv <= 16 and nv - nconsm <= 8. */
 int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
                                        const void* wbf16, const float* params, const float* norm,
-                                       const float* guard, int32_t* fallbacks, int32_t grid, void* stream);
+                                       const float* guard, const float* rate, int32_t* fallbacks, int32_t grid,
+                                       void* stream);
 /* The same step with the MLP on the 5th-generation tensor cores: 128 nodes
  * per block tile, one node per thread, the three layers as tcgen05 MMAs with
  * FP32 accumulators in tensor memory; BF16 weights from the FP32 master block
- * params (no BF16 copy needed).  Same guard and fallback count; the
- * corrections equal those of the warp-level kernel up to the FP32
+ * params (no BF16 copy needed).  Same guard, rate form and fallback count;
+ * the corrections equal those of the warp-level kernel up to the FP32
  * accumulation order inside a layer. */
 int lbm_one_time_step_periodic_closure_tc(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
                                           const float* params, const float* norm, const float* guard,
-                                          int32_t* fallbacks, void* stream);
+                                          const float* rate, int32_t* fallbacks, void* stream);
 
 /* Pure pull streaming on the interior (pylbm/algorithm/base.py:289-296). */
 int lbm_transport(const void* f, void* fnew, const lbm_lattice* lat, void* stream);

@@ -216,13 +216,23 @@ class Mlp:
 # ---------------------------------------------------------------------------
 class ClosureModel:
     """A trained closure: MLP parameters and the normalisation of its inputs
-    (pre-collision moments) and outputs (non-conserved moment corrections)."""
+    (pre-collision moments) and outputs (non-conserved moment corrections).
 
-    def __init__(self, params, norm, meta=None, seed=0):
+    ``rate`` (16 floats lo[8], hi[8], or None): the rate form of the fused
+    step, in which output j sets lam_j in [lo_j, hi_j] and the node relaxes
+    moment j at s_j (1 + lam_j) instead of adding y_j sig_j + mu_j.
+    """
+
+    def __init__(self, params, norm, meta=None, seed=0, rate=None):
         self.mlp = Mlp(seed=seed, params=params)
         self.norm = np.ascontiguousarray(norm, dtype=np.float32)
         if self.norm.size != 48:
             raise ValueError("norm holds mu_in[16], isig_in[16], mu_out[8], sig_out[8]")
+        self.rate = None
+        if rate is not None:
+            self.rate = np.ascontiguousarray(rate, dtype=np.float32)
+            if self.rate.size != 16 or np.any(self.rate[:8] > self.rate[8:]) or np.any(self.rate[:8] < -1.0):
+                raise ValueError("rate holds lo[8], hi[8] with -1 <= lo <= hi")
         self.meta = dict(meta or {})
         sm, _ = runtime.device_info()
         self.grid = 2 * sm  # fused closure step: persistent blocks, two per SM
@@ -237,15 +247,23 @@ class ClosureModel:
     def guard_ptr(self):
         return self.guard.ctypes.data_as(ctypes.c_void_p)
 
+    def rate_ptr(self):
+        return None if self.rate is None else self.rate.ctypes.data_as(ctypes.c_void_p)
+
     def save(self, path):
-        np.savez(path, params=self.mlp.params_host(), norm=self.norm,
-                 meta=np.array(repr(self.meta)))
+        extra = {} if self.rate is None else {"rate": self.rate}
+        np.savez(path, params=self.mlp.params_host(), norm=self.norm, guard=self.guard,
+                 meta=np.array(repr(self.meta)), **extra)
 
     @classmethod
     def load(cls, path):
         d = np.load(path, allow_pickle=False)
         import ast
-        return cls(d["params"], d["norm"], ast.literal_eval(str(d["meta"])))
+        model = cls(d["params"], d["norm"], ast.literal_eval(str(d["meta"])),
+                    rate=d["rate"] if "rate" in d.files else None)
+        if "guard" in d.files:
+            model.guard = np.ascontiguousarray(d["guard"], dtype=np.float32)
+        return model
 
 
 def _restrict(sim, factor):

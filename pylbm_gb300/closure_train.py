@@ -76,13 +76,14 @@ class CoarseStep:
         return torch.stack(out, dim=1)
 
     def __call__(self, f, closure=None):
-        """One time step; ``closure(m_pre)`` returns corrections (batch, nv - nc, n0, n1)."""
+        """One time step; ``closure(m_pre, m_relaxed)`` returns corrections
+        (batch, nv - nc, n0, n1) of the non-conserved moments."""
         m = self.moments(self.pull(f))
         meq = self.equilibrium(m)
         r = self.rates.view(1, -1, 1, 1)
         relaxed = m + r * (meq - m)
         if closure is not None:
-            corr = closure(m)
+            corr = closure(m, relaxed)
             relaxed = torch.cat([relaxed[:, :self.nc], relaxed[:, self.nc:] + corr], dim=1)
         return self.populations(relaxed)
 
@@ -107,13 +108,15 @@ class _MlpOnKernels(torch.autograd.Function):
 
 
 class KernelClosure:
-    """The closure of a ClosureModel as a differentiable map m_pre -> corrections."""
+    """The closure of a ClosureModel as a differentiable map (m_pre, m_relaxed)
+    -> corrections, in the additive or the rate form of the fused step."""
 
     def __init__(self, model, device):
         self.model = model
         nrm = torch.tensor(model.norm, dtype=torch.float32, device=device)
         self.mu_in, self.isig_in = nrm[0:16], nrm[16:32]
         self.mu_out, self.sig_out = nrm[32:40], nrm[40:48]
+        self.rate = None if model.rate is None else torch.tensor(model.rate, dtype=torch.float32, device=device)
         self.anchor = torch.zeros(1, device=device, requires_grad=True)
 
     def inputs(self, m):
@@ -124,12 +127,16 @@ class KernelClosure:
         x[:, :nv] = (rows - self.mu_in[:nv]) * self.isig_in[:nv]
         return x.to(torch.bfloat16).contiguous()
 
-    def __call__(self, m):
+    def __call__(self, m, relaxed):
         b, nv, n0, n1 = m.shape
         nn = nv - 3
         y = _MlpOnKernels.apply(self.anchor, self.inputs(m), self.model.mlp)
-        corr = y[:, :nn] * self.sig_out[:nn] + self.mu_out[:nn]
-        return corr.reshape(b, n0, n1, nn).permute(0, 3, 1, 2).to(m.dtype)
+        z = (y[:, :nn] * self.sig_out[:nn] + self.mu_out[:nn]).reshape(b, n0, n1, nn).permute(0, 3, 1, 2)
+        if self.rate is None:
+            return z.to(m.dtype)
+        lo, hi = self.rate[:nn].view(1, -1, 1, 1), self.rate[8:8 + nn].view(1, -1, 1, 1)
+        lam = lo + (hi - lo) * torch.sigmoid(z)
+        return lam.to(m.dtype) * (relaxed[:, 3:] - m[:, 3:])
 
 
 def vorticity(cons):
@@ -206,6 +213,115 @@ def rollout_errors(model, seeds, finals, t_coarse, n=256, re=30000.0):
         e = float(np.linalg.norm(w - w_ref) / np.linalg.norm(w_ref))
         errs.append(e if bad == 0 and np.isfinite(e) else float("inf"))
     return errs
+
+
+def reference_trajectories(seeds, t_end, every, n_fine=1024, factor=4, re=30000.0, device="cuda", log=None):
+    """The coarse runs' own initial populations and the restricted fine
+    conserved moments every ``every`` coarse steps up to ``t_end``.
+
+    Returns (inits (S, 9, n, n), refs (S, t_end // every, 3, n, n)) as
+    float32 tensors on ``device``; refs[:, i] belongs to coarse step
+    (i + 1) * every.
+    """
+    from .simulation import Simulation
+
+    inits, refs = [], []
+    t0 = time.time()
+    n = n_fine // factor
+    for s in seeds:
+        coarse = Simulation(study_dicos(int(s), n, re), dtype="float32")
+        inits.append(torch.tensor(np.array([coarse.F[k] for k in range(coarse.scheme.nv)]), dtype=torch.float32))
+        coarse.free()
+        sim = Simulation(study_dicos(int(s), n_fine, re), dtype="float64", parity=False)
+        M3 = np.asarray(sim.scheme.M, dtype=np.float64)[:3]
+        seq = []
+        for _ in range(t_end // every):
+            sim.run(factor * every)
+            seq.append(np.einsum("ij,j...->i...", M3, _restrict(sim, factor)))
+        sim.free()
+        refs.append(torch.tensor(np.array(seq), dtype=torch.float32).to(device))
+        if log:
+            log(f"seed {s}: {len(seq)} reference snapshots, {time.time() - t0:.1f}s")
+    return torch.stack(inits).to(device), torch.stack(refs)
+
+
+def _snapshot_error(step, f, ref):
+    cons = step.moments(f)[:, :3]
+    ref = ref.to(step.dtype)
+    w, w_ref = vorticity(cons), vorticity(ref)
+    ew = ((w - w_ref) ** 2).sum(dim=(1, 2)) / (w_ref ** 2).sum(dim=(1, 2))
+    eq = ((cons[:, 1:] - ref[:, 1:]) ** 2).sum(dim=(1, 2, 3)) / (ref[:, 1:] ** 2).sum(dim=(1, 2, 3))
+    return (ew + eq).mean()
+
+
+def train_on_trajectories(model, inits, refs, every, segment=16, episodes=8, batch=4, lr=1e-3, clip=1.0,
+                          log=None, seed=0, rollout=None, scheme=None):
+    """Truncated backpropagation along the closure run's own trajectory.
+
+    Each episode starts ``batch`` coarse runs from their own initial states
+    and advances them with the closure over the whole reference window; every
+    ``segment`` steps the error against the restricted fine moments at the
+    snapshots inside the segment is back-propagated through that segment's
+    steps only (the state entering it is a constant) and Adam takes a step.
+    The start states are thus always states of the closure run itself, the
+    ones the trained closure meets when it runs.  ``rollout``: as in
+    train_aposteriori (validation over whole runs, best parameters kept).
+    """
+    if segment % every:
+        raise ValueError("segment must be a multiple of the snapshot spacing")
+    device = inits.device
+    step = CoarseStep(scheme or Scheme(study_dicos(0, inits.shape[-1])), device=device)
+    closure = KernelClosure(model, device)
+    mlp = model.mlp
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    t_end = refs.shape[1] * every
+    nseg = t_end // segment
+    total = episodes * nseg
+    history, best, it = [], (float("inf"), None), 0
+    if rollout is not None:
+        errs = rollout(model)
+        best = (float(np.mean(errs)), mlp.params_host())
+        history.append({"episode": 0, "rollout": errs})
+        if log:
+            log(json.dumps(history[-1]))
+    mlp.g.zero(mlp.stream)
+    for ep in range(episodes):
+        idx = torch.randperm(inits.shape[0], generator=gen)[:batch].to(device)
+        f = inits[idx].clone()
+        losses = []
+        for sgi in range(nseg):
+            f = f.detach()
+            loss = 0.0
+            for k in range(segment):
+                f = step(f, closure)
+                t = sgi * segment + k + 1
+                if t % every == 0:
+                    loss = loss + _snapshot_error(step, f, refs[idx, t // every - 1])
+            loss.backward()
+            torch.cuda.synchronize()
+            g = mlp.grad_host()
+            gn = float(np.linalg.norm(g))
+            if math.isfinite(gn):
+                if gn > clip:
+                    mlp.set_grad(g * (clip / gn))
+                mlp.adam_step(lr * 0.5 * (1.0 + math.cos(math.pi * it / total)))
+            else:
+                mlp.g.zero(mlp.stream)
+            it += 1
+            losses.append(float(loss.detach()))
+        rec = {"episode": ep + 1, "loss_first": losses[0], "loss_last": losses[-1], "loss_mean": float(np.mean(losses))}
+        if rollout is not None:
+            errs = rollout(model)
+            rec["rollout"] = errs
+            if float(np.mean(errs)) < best[0]:
+                best = (float(np.mean(errs)), mlp.params_host())
+        history.append(rec)
+        if log:
+            log(json.dumps(rec))
+    if best[1] is not None:
+        mlp.set_params(best[1])
+        history.append({"kept_rollout_mean": best[0]})
+    return history
 
 
 def segment_loss(step, closure, f0, targets):
@@ -335,6 +451,60 @@ def rescale_outputs(model, scales, open_all=False):
     return out
 
 
+def _input_norm(step, starts):
+    norm = np.zeros(48, np.float32)
+    with torch.no_grad():
+        m = step.moments(step.pull(starts[:8]))
+        mu = m.mean(dim=(0, 2, 3)).cpu().numpy()
+        sd = m.std(dim=(0, 2, 3)).cpu().numpy()
+    nv = mu.size
+    norm[:nv] = mu
+    norm[16:16 + nv] = np.where(sd > 0, 1.0 / np.maximum(sd, 1e-30), 0.0)
+    return norm
+
+
+def additive_model(step, starts):
+    """A fresh additive-form network whose corrections start at zero."""
+    norm = _input_norm(step, starts)
+    norm[40:40 + step.nv - step.nc] = output_scales(step, starts)
+    p = init_params(0)
+    p[W3_AT:B3_AT] = 0.0  # zero last layer: the closure starts as the plain step
+    return ClosureModel(p, norm, {"form": "additive"})
+
+
+def rate_bounds(rates, rate_max=1.9995, lam_lo=-0.3, lam_lo_stress=-0.02, lam_hi=0.3):
+    """(lo[8], hi[8]) of lam per non-conserved moment: the effective rate
+    s (1 + lam) stays at most ``rate_max``; moments relaxed near 2 (above
+    1.9: the stresses at low viscosity) get the tighter lower bound."""
+    lo = np.zeros(8, np.float32)
+    hi = np.zeros(8, np.float32)
+    for j, sj in enumerate(rates):
+        if sj <= 0.0:
+            continue
+        lo[j] = lam_lo_stress if sj > 1.9 else lam_lo
+        hi[j] = min(lam_hi, rate_max / sj - 1.0)
+        if hi[j] <= lo[j]:
+            hi[j] = lo[j] = 0.0
+    return lo, hi
+
+
+def rate_model(step, starts, rate_max=1.9995, lam_lo=-0.3, lam_lo_stress=-0.02, lam_hi=0.3):
+    """A fresh rate-form network: zero last layer and mu_out at the logit
+    where lam = 0, so it starts as the plain step."""
+    norm = _input_norm(step, starts)
+    rates = step.rates[step.nc:].cpu().numpy()
+    lo, hi = rate_bounds(rates, rate_max, lam_lo, lam_lo_stress, lam_hi)
+    for j in range(rates.size):
+        if hi[j] > lo[j]:
+            frac = -lo[j] / (hi[j] - lo[j])
+            norm[32 + j] = float(np.log(frac / (1.0 - frac)))
+            norm[40 + j] = 1.0
+    p = init_params(0)
+    p[W3_AT:B3_AT] = 0.0
+    model = ClosureModel(p, norm, {"form": "rate", "rate_max": rate_max}, rate=np.concatenate([lo, hi]))
+    return model
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--seeds", type=int, default=48, help="training seeds (fine float64 runs)")
@@ -346,47 +516,65 @@ def main():
     ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--report-every", type=int, default=100)
     ap.add_argument("--init", default=None, help="start from this model (else a fresh network)")
-    ap.add_argument("--all-outputs", action="store_true", help="correct all six non-conserved moments")
+    ap.add_argument("--all-outputs", action="store_true", help="additive form: correct all six non-conserved moments")
+    ap.add_argument("--form", default="rate", choices=["rate", "additive"])
+    ap.add_argument("--rate-max", type=float, default=1.9995, help="rate form: largest effective rate")
+    ap.add_argument("--lam-lo", type=float, default=-0.3, help="rate form: lower bound of lam")
+    ap.add_argument("--lam-lo-stress", type=float, default=-0.02,
+                    help="rate form: lower bound of lam for moments relaxed near 2 (the stresses)")
+    ap.add_argument("--lam-hi", type=float, default=0.3, help="rate form: upper bound of lam (before --rate-max)")
     ap.add_argument("--out", required=True)
     ap.add_argument("--eval-seeds", type=int, default=20)
     ap.add_argument("--t-coarse", type=int, default=1500)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--mode", default="trajectory", choices=["trajectory", "segments"],
+                    help="trajectory: truncated backpropagation along the closure run's own trajectory; "
+                         "segments: unrolls started from restricted fine states")
+    ap.add_argument("--episodes", type=int, default=8)
+    ap.add_argument("--every", type=int, default=4, help="trajectory mode: coarse steps between reference snapshots")
     args = ap.parse_args()
     log = lambda s: print(s, flush=True)  # noqa: E731
     t0 = time.time()
     times = [int(t) for t in args.times.split(",")]
-    starts, targets = trajectory_data(range(args.seeds), times, args.unroll, log=log)
     vseeds = range(50000, 50000 + args.val_seeds)
     vstarts, vtargets, vfinals = trajectory_data(vseeds, times, args.unroll, final=args.t_coarse)
-    log(f"data: {starts.shape[0]} segments of {args.unroll} steps in {time.time() - t0:.1f}s")
+    if args.mode == "segments":
+        starts, targets = trajectory_data(range(args.seeds), times, args.unroll, log=log)
+        log(f"data: {starts.shape[0]} segments of {args.unroll} steps in {time.time() - t0:.1f}s")
+    else:
+        inits, refs = reference_trajectories(range(args.seeds), args.t_coarse, args.every, log=log)
+        starts = vstarts  # normalisation statistics
+        log(f"data: {inits.shape[0]} trajectories of {args.t_coarse} steps in {time.time() - t0:.1f}s")
     step = CoarseStep(Scheme(study_dicos(0, starts.shape[-1])), device=starts.device)
     if args.init:
         model = ClosureModel.load(args.init)
+        if (model.rate is not None) != (args.form == "rate"):
+            raise SystemExit(f"--init holds a model of the other form than --form {args.form}")
+        if args.form == "additive":
+            model = rescale_outputs(model, output_scales(step, starts), open_all=args.all_outputs)
+    elif args.form == "rate":
+        model = rate_model(step, starts, args.rate_max, args.lam_lo, args.lam_lo_stress, args.lam_hi)
     else:
-        scales = output_scales(step, starts)
-        norm = np.zeros(48, np.float32)
-        with torch.no_grad():
-            m = step.moments(step.pull(starts[:8]))
-            mu = m.mean(dim=(0, 2, 3)).cpu().numpy()
-            sd = m.std(dim=(0, 2, 3)).cpu().numpy()
-        norm[:9] = mu
-        norm[16:25] = np.where(sd > 0, 1.0 / np.maximum(sd, 1e-30), 0.0)
-        norm[40:46] = scales
-        p = init_params(0)
-        p[W3_AT:B3_AT] = 0.0  # zero last layer: the closure starts as the plain step
-        model = ClosureModel(p, norm, {})
-    model = rescale_outputs(model, output_scales(step, starts), open_all=args.all_outputs)
+        model = additive_model(step, starts)
     plain = plain_validation(vstarts, vtargets)
     closure = KernelClosure(model, starts.device)
     before = validation(step, closure, vstarts, vtargets)
     log(json.dumps({"val_plain": plain, "val_closure_before": before}))
-    history = train_aposteriori(model, starts, targets, iters=args.iters, batch=args.batch, lr=args.lr,
-                                val=(vstarts, vtargets), log=log, report_every=args.report_every,
-                                rollout=lambda mdl: rollout_errors(mdl, vseeds, vfinals, args.t_coarse))
-    model.meta.update({"training": "a-posteriori", "unroll": args.unroll, "seeds": args.seeds, "times": times,
-                       "re": 30000.0, "n_fine": 1024, "factor": 4, "iters": args.iters})
+    rollout = lambda mdl: rollout_errors(mdl, vseeds, vfinals, args.t_coarse)  # noqa: E731
+    if args.mode == "segments":
+        history = train_aposteriori(model, starts, targets, iters=args.iters, batch=args.batch, lr=args.lr,
+                                    val=(vstarts, vtargets), log=log, report_every=args.report_every,
+                                    rollout=rollout)
+    else:
+        history = train_on_trajectories(model, inits, refs, args.every, segment=args.unroll,
+                                        episodes=args.episodes, batch=args.batch, lr=args.lr, log=log,
+                                        rollout=rollout)
+    model.meta.update({"training": "a-posteriori, " + args.mode, "unroll": args.unroll, "seeds": args.seeds,
+                       "re": 30000.0, "n_fine": 1024, "factor": 4, "lr": args.lr,
+                       **({"times": times, "iters": args.iters} if args.mode == "segments" else
+                          {"episodes": args.episodes, "every": args.every, "t_coarse": args.t_coarse})})
     model.save(args.out)
-    del starts, targets
+    del starts
     torch.cuda.empty_cache()
     log(f"model saved to {args.out} after {time.time() - t0:.1f}s")
     rows, summary = [], {}

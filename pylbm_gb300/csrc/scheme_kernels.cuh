@@ -771,9 +771,31 @@ struct ClosureArgs {
   // plain MRT collision and is counted (ratio <= 0: no guard)
   float guard_ratio, guard_floor;
   int* fallbacks;          // device counter of guarded nodes, or null
+  // rate form (rate_form != 0): output j scales the relaxation's own change
+  // of moment j, corr_j = lam_j (m_relaxed_j - m_j) with
+  // lam_j = lam_lo[j] + (lam_hi[j] - lam_lo[j]) sigmoid(y_j sig_out[j] + mu_out[j]),
+  // so the effective rate s_j (1 + lam_j) stays inside the caller's bounds
+  int rate_form;
+  float lam_lo[8], lam_hi[8];
 };
 
+// correction of non-conserved moment j from the network output y (bias
+// included) and the relaxation's change d of that moment
+__device__ __forceinline__ float closure_correction(const ClosureArgs& c, int j, float y, float d) {
+  const float z = y * c.sig_out[j] + c.mu_out[j];
+  if (!c.rate_form) return z;
+  const float lam = c.lam_lo[j] + (c.lam_hi[j] - c.lam_lo[j]) / (1.0f + __expf(-z));
+  return lam * d;
+}
+
 constexpr int kClosureWarps = 8;
+// nodes per warp and pass: 32 (every lane pulls, relaxes and stores a node;
+// the MLP runs as two 16-row tiles) or 16 (lanes 16..31 only join the MLP)
+#ifndef LBM_CLOSURE_WARP_NODES
+#define LBM_CLOSURE_WARP_NODES 32
+#endif
+constexpr int kClosureWarpNodes = LBM_CLOSURE_WARP_NODES;
+static_assert(kClosureWarpNodes == 16 || kClosureWarpNodes == 32, "16 or 32 nodes per warp");
 #ifndef LBM_CLOSURE_MIN_BLOCKS
 // no register cap: capping at 64 or 80 registers spills and was slower
 #define LBM_CLOSURE_MIN_BLOCKS 1
@@ -787,7 +809,7 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
   __shared__ __align__(16) __nv_bfloat16 w_s[BW2N];
   __shared__ float b_s[2 * H + OUT];
   __shared__ __align__(16) __nv_bfloat16 x_s[kClosureWarps][32 * IN];
-  __shared__ float y_s[kClosureWarps][16 * OUT];
+  __shared__ float y_s[kClosureWarps][kClosureWarpNodes * OUT];
   static_assert((BW2N * sizeof(__nv_bfloat16)) % 16 == 0, "weight block must be a whole number of 16-byte words");
   {
     const uint4* src = reinterpret_cast<const uint4*>(c.w);
@@ -803,12 +825,13 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   const Geo& g = a.g;
-  // 16 nodes per warp (one 16-row MMA tile): lanes 0..15 own a node, all 32
-  // lanes evaluate the MLP; short per-warp chains, twice the warps in flight
-  const long long per_block = 16 * kClosureWarps;
+  // kClosureWarpNodes nodes per warp: lane l owns node l of the warp's run
+  // (l < kClosureWarpNodes); all 32 lanes evaluate the MLP, one 16-row MMA
+  // tile after the other
+  const long long per_block = kClosureWarpNodes * kClosureWarps;
   for (long long base = (long long)blockIdx.x * per_block; base < c.nodes; base += (long long)gridDim.x * per_block) {
-    const long long node = base + warp * 16 + lane;
-    const bool active = lane < 16 && node < c.nodes;
+    const long long node = base + warp * kClosureWarpNodes + lane;
+    const bool active = lane < kClosureWarpNodes && node < c.nodes;
     int idx[3] = {0, 0, 0};
     long long q = active ? node : 0;
     for (int d = LBM_DIM - 1; d >= 0; --d) {
@@ -836,7 +859,7 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
       for (int k = 0; k < LBM_Q; ++k) m[k] = (R)0;
     }
     // normalised pre-collision moments (absolute values) -> BF16 row of this lane
-    if (lane < 16) {
+    if (lane < kClosureWarpNodes) {
       __nv_bfloat16* xr = &x_s[warp][lane * IN];
 #pragma unroll
       for (int k = 0; k < IN; ++k) {
@@ -847,8 +870,9 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
       }
     }
     __syncwarp();
-    {
-      const __nv_bfloat16* xt = &x_s[warp][0];
+#pragma unroll 1
+    for (int t = 0; t < kClosureWarpNodes / 16; ++t) {
+      const __nv_bfloat16* xt = &x_s[warp][t * 16 * IN];
       uint32_t xa[4];
       xa[0] = *reinterpret_cast<const uint32_t*>(xt + gq * IN + 2 * tq);
       xa[1] = *reinterpret_cast<const uint32_t*>(xt + (gq + 8) * IN + 2 * tq);
@@ -857,7 +881,7 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
       float y[4], z1[8][4], z2[8][4];
       uint32_t h1a[4][4], h2a[4][4];
       forward_tile<false>(xa, w_s, b_s, b_s + H, b_s + 2 * H, lane, y, z1, z2, h1a, h2a);
-      float* yt = &y_s[warp][0];
+      float* yt = &y_s[warp][t * 16 * OUT];
       yt[gq * OUT + 2 * tq] = y[0];
       yt[gq * OUT + 2 * tq + 1] = y[1];
       yt[(gq + 8) * OUT + 2 * tq] = y[2];
@@ -873,8 +897,9 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
       float change = 0.0f;
 #pragma unroll
       for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) {
-        corr[j] = y_s[warp][lane * OUT + j] * c.sig_out[j] + c.mu_out[j];
-        change = fmaxf(change, fabsf((float)(m[LBM_NCONS + j] - pre[j])));
+        const float d = (float)(m[LBM_NCONS + j] - pre[j]);
+        corr[j] = closure_correction(c, j, y_s[warp][lane * OUT + j], d);
+        change = fmaxf(change, fabsf(d));
       }
       bool ok = true;
       if (c.guard_ratio > 0.0f) {
@@ -1048,8 +1073,9 @@ __global__ void __launch_bounds__(kTcRows) k_step_periodic_closure_tc(const S* _
       float change = 0.0f;
 #pragma unroll
       for (int j = 0; j < LBM_Q - LBM_NCONS; ++j) {
-        corr[j] = (y[j] + sm.b3[j]) * c.sig_out[j] + c.mu_out[j];
-        change = fmaxf(change, fabsf((float)(m[LBM_NCONS + j] - pre[j])));
+        const float d = (float)(m[LBM_NCONS + j] - pre[j]);
+        corr[j] = closure_correction(c, j, y[j] + sm.b3[j], d);
+        change = fmaxf(change, fabsf(d));
       }
       bool keep = true;
       if (c.guard_ratio > 0.0f) {
@@ -1618,26 +1644,27 @@ int lbm_source_term(double* m, const lbm_lattice* mlat, const double* prm, void*
 }
 
 static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, const void* wbf16,
-                          const float* params, const float* norm, const float* guard, int32_t* fallbacks,
-                          int32_t grid, void* stream, bool tc, const char* who);
+                          const float* params, const float* norm, const float* guard, const float* rate,
+                          int32_t* fallbacks, int32_t grid, void* stream, bool tc, const char* who);
 
 int lbm_one_time_step_periodic_closure(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
                                        const void* wbf16, const float* params, const float* norm,
-                                       const float* guard, int32_t* fallbacks, int32_t grid, void* stream) {
-  return closure_common(f, fnew, lat, prm, wbf16, params, norm, guard, fallbacks, grid, stream, false,
+                                       const float* guard, const float* rate, int32_t* fallbacks, int32_t grid,
+                                       void* stream) {
+  return closure_common(f, fnew, lat, prm, wbf16, params, norm, guard, rate, fallbacks, grid, stream, false,
                         "lbm_one_time_step_periodic_closure");
 }
 
 int lbm_one_time_step_periodic_closure_tc(const void* f, void* fnew, const lbm_lattice* lat, const double* prm,
                                           const float* params, const float* norm, const float* guard,
-                                          int32_t* fallbacks, void* stream) {
-  return closure_common(f, fnew, lat, prm, nullptr, params, norm, guard, fallbacks, 0, stream, true,
+                                          const float* rate, int32_t* fallbacks, void* stream) {
+  return closure_common(f, fnew, lat, prm, nullptr, params, norm, guard, rate, fallbacks, 0, stream, true,
                         "lbm_one_time_step_periodic_closure_tc");
 }
 
 static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, const double* prm, const void* wbf16,
-                          const float* params, const float* norm, const float* guard, int32_t* fallbacks,
-                          int32_t grid, void* stream, bool tc, const char* who) {
+                          const float* params, const float* norm, const float* guard, const float* rate,
+                          int32_t* fallbacks, int32_t grid, void* stream, bool tc, const char* who) {
   using namespace lbm_scheme;
   int rc = check_pop_lattice(lat, who);
   if (rc) return rc;
@@ -1662,6 +1689,14 @@ static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, con
   c.guard_ratio = guard ? guard[0] : 0.0f;
   c.guard_floor = guard ? guard[1] : 0.0f;
   c.fallbacks = fallbacks;
+  c.rate_form = rate != nullptr;
+  for (int i = 0; i < 8; ++i) {
+    c.lam_lo[i] = rate ? rate[i] : 0.0f;
+    c.lam_hi[i] = rate ? rate[8 + i] : 0.0f;
+    if (rate && !(c.lam_lo[i] <= c.lam_hi[i] && c.lam_lo[i] >= -1.0f))
+      return lbm::fail(LBM_ERR_ARG, "%s: rate bounds of output %d: [%g, %g] (need -1 <= lo <= hi)", who, i,
+                       (double)c.lam_lo[i], (double)c.lam_hi[i]);
+  }
 #if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
   if (tc) {
     int dev = 0, sms = 0;
@@ -1678,7 +1713,7 @@ static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, con
     return lbm::launch_check(who);
   }
 #endif
-  const long long per = 16 * kClosureWarps;
+  const long long per = kClosureWarpNodes * kClosureWarps;
   long long blocks = (c.nodes + per - 1) / per;
   if (grid > 0 && blocks > grid) blocks = grid;
   k_step_periodic_closure<<<(unsigned)blocks, 32 * kClosureWarps, 0, (cudaStream_t)stream>>>((const S*)f, (S*)fnew,

@@ -487,8 +487,8 @@ class SchemeModule:
         _sig(lib, "lbm_scheme_closure_tc_occupancy", I32, [ctypes.POINTER(ctypes.c_int32)] * 2)
         _sig(lib, "lbm_ensemble_step", I32, [P, P, P, I32, I32, I32, I32, I32, P])
         _sig(lib, "lbm_ensemble_step_pairs", I32, [P, P, P, I32, I32, I32, I32, I32, P])
-        _sig(lib, "lbm_one_time_step_periodic_closure", I32, [P, P, LP, P, P, P, P, P, P, I32, P])
-        _sig(lib, "lbm_one_time_step_periodic_closure_tc", I32, [P, P, LP, P, P, P, P, P, P])
+        _sig(lib, "lbm_one_time_step_periodic_closure", I32, [P, P, LP, P, P, P, P, P, P, P, I32, P])
+        _sig(lib, "lbm_one_time_step_periodic_closure_tc", I32, [P, P, LP, P, P, P, P, P, P, P])
 
     def call(self, rc):
         check(rc, self.lib, "lbm_scheme_last_error")

@@ -610,12 +610,13 @@ class Simulation:
             # the MLP on the 5th-generation tensor cores, one node per thread
             self.module.call(self.module.lib.lbm_one_time_step_periodic_closure_tc(
                 F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.p.handle, model.norm_ptr(),
-                model.guard_ptr(), self._fallbacks.handle, self._stream))
+                model.guard_ptr(), model.rate_ptr(), self._fallbacks.handle, self._stream))
             return
         if model is not None:
             self.module.call(self.module.lib.lbm_one_time_step_periodic_closure(
                 F.handle, Fnew.handle, ctypes.byref(self._lat), pp, model.mlp.w.handle, model.mlp.p.handle,
-                model.norm_ptr(), model.guard_ptr(), self._fallbacks.handle, model.grid, self._stream))
+                model.norm_ptr(), model.guard_ptr(), model.rate_ptr(), self._fallbacks.handle, model.grid,
+                self._stream))
             return
         fn = self.module.lib.lbm_one_time_step_periodic if self.periodic else self.module.lib.lbm_one_time_step
         self.module.call(fn(F.handle, Fnew.handle, ctypes.byref(self._lat), pp, self._stream))

@@ -35,7 +35,7 @@ def test_coarse_step_closure_adds_to_non_conserved_moments_only():
     f = torch.tensor(_interior(o))[None]
     corr = torch.full((1, 6, 16, 16), 1e-3, dtype=torch.float64)
     a = step.moments(step(f))
-    b = step.moments(step(f, lambda m: corr))
+    b = step.moments(step(f, lambda m, relaxed: corr))
     assert torch.allclose(a[:, :3], b[:, :3], rtol=0, atol=1e-15)
     assert torch.allclose(b[:, 3:] - a[:, 3:], corr, rtol=0, atol=1e-14)
 

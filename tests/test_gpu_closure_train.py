@@ -24,15 +24,31 @@ def _populations(sim):
     return np.array([sim.F[k] for k in range(sim.scheme.nv)])
 
 
-def test_unrolled_step_matches_cuda_closure_step():
+def _rate_model(sim, seed=3):
+    """A random rate-form network with the training's bounds for this scheme."""
+    from pylbm_gb300.closure_train import rate_bounds
+    base = _model(seed=seed)
+    lo, hi = rate_bounds(sim.scheme.rates_numpy()[3:])
+    norm = base.norm.copy()
+    norm[40:46] = 1.0
+    return ClosureModel(base.mlp.params_host(), norm, {}, rate=np.concatenate([lo, hi]))
+
+
+@pytest.mark.parametrize("form,kernel", [("additive", "tc"), ("additive", "warp"), ("rate", "tc"),
+                                         ("rate", "warp")])
+def test_unrolled_step_matches_cuda_closure_step(form, kernel):
+    """The restatement (float64 step, MLP on lbm_mlp_forward_tc) against the
+    fused CUDA closure step over 12 steps, in both output forms: the
+    additive corrections, and the rate form (the node relaxes moment j at
+    s_j (1 + lam_j), lam_j bounded)."""
     n, steps = 64, 12
-    model = _model()
     sim = Simulation(study_dicos(5, n, re=3000.0), dtype="float32")
+    model = _model() if form == "additive" else _rate_model(sim)
     # the restatement in float64: absolute FP32 populations (~0.1-0.4 each)
     # would round q about as much as the closure changes it in 12 steps
     f0 = torch.tensor(_populations(sim), dtype=torch.float64, device="cuda")[None]
     sim.set_closure(model)
-    sim.closure_kernel = "tc"
+    sim.closure_kernel = kernel
     sim.run(steps)
     got = np.array([sim.m[k] for k in range(3)])
     step = CoarseStep(sim.scheme, device="cuda", dtype=torch.float64)
