@@ -22,7 +22,28 @@ pre-collision moments rounded to BF16, corrections are added after the
 relaxation, rho and q are never changed.  The trained model is evaluated
 with the CUDA closure step (closure_study.evaluate), not with this restatement.
 
-    python -m pylbm_gb300.closure_train [--seeds 64] [--unroll 16] [--iters 1500] [--init model.npz] [--out model.npz]
+Two ways to choose the unrolled segments:
+
+* ``--mode trajectory`` (default): truncated backpropagation along the
+  closure run's own trajectory.  Each episode advances a batch of coarse runs
+  from their own initial states over the whole window; every ``--unroll``
+  steps the error against the restricted fine moments is back-propagated
+  through that segment and Adam steps.  The segments start from the states
+  the closure meets when it runs.
+* ``--mode segments``: unrolls started from restricted fine states.  Their
+  short-horizon loss falls while the whole run gets worse: the network
+  learns to undo the start-up transient of a restricted fine state, which a
+  coarse run never has.
+
+Two output forms (``--form``): ``additive`` (the correction is the scaled
+output) and ``rate`` (the output sets lam_j in bounds and the node relaxes
+moment j at s_j (1 + lam_j); with every effective rate below 2 the
+collision cannot turn unstable, which the additive form did when its
+corrections pushed the stress relaxation past 2).  Every report validates
+the model over whole runs with the CUDA closure step and the best
+parameters are kept.
+
+    python -m pylbm_gb300.closure_train --out model.npz [--mode trajectory] [--form rate] [--seeds 24]
 """
 import argparse
 import json

@@ -1,10 +1,13 @@
 """What the trained closure gains over the plain coarse method (held-out seed).
 
-The model in pylbm_gb300/data was trained by pylbm_gb300.closure_study on
-200 seeds of the Re 30 000 double shear layer (1024^2 float64 runs restricted
-4x); seed 100000 was not among them.  After 1500 coarse steps, the learned
-256^2 run must be closer to the float64 1024^2 solution than the plain 256^2
-run, with mass and momentum conserved.
+The model in pylbm_gb300/data was trained by pylbm_gb300.closure_train
+(rate form, truncated backpropagation along the closure run's own
+trajectory) on seeds 0..31 of the Re 30 000 double shear layer (1024^2
+float64 runs restricted 4x); seed 100000 was not among them.  After 1500
+coarse steps the learned 256^2 run must be within 2 % (vorticity relative
+L2) of the float64 1024^2 solution, well below the plain 256^2 run and below
+plain 256^2 with the viscosity lowered by the best uniform factor (0.8), with
+mass and momentum conserved and no node falling back to the plain collision.
 """
 import numpy as np
 import pytest
@@ -38,7 +41,13 @@ def test_learned_closure_beats_plain_coarse_on_held_out_seed():
     learned.run(steps)
     c1 = learned.conserved_sums()
     err_learned = np.linalg.norm(_vort(learned, 1) - w_ref) / np.linalg.norm(w_ref)
-    assert err_learned < 0.97 * err_plain, (err_learned, err_plain)
+    retuned = Simulation(study_dicos(seed, 256, re=30000.0 / 0.8), dtype="float32")
+    retuned.run(steps)
+    err_retuned = np.linalg.norm(_vort(retuned, 1) - w_ref) / np.linalg.norm(w_ref)
+    print(f"plain {err_plain:.4f}, retuned {err_retuned:.4f}, learned {err_learned:.4f}")
+    assert err_learned < 0.02
+    assert err_learned < 0.6 * err_plain, (err_learned, err_plain)
+    assert err_learned < 0.8 * err_retuned, (err_learned, err_retuned)
     # the trained network never trips the fused step's guard
     assert learned.closure_fallbacks() == 0
     assert abs(c1[0] - c0[0]) < 1e-6 * abs(c0[0])
