@@ -583,10 +583,12 @@ class Simulation:
             raise ValueError("the learned closure corrects the plain MRT relaxation only")
         self.closure = model
         if not hasattr(self, "closure_kernel"):
-            # "tc": tcgen05 MMAs, 128 nodes per block; "warp": mma.sync, 16 nodes
-            # per warp; "auto": the tensor-core step from 2^18 interior nodes on
-            # (the warp kernel is faster on smaller grids, where a block's
-            # set-up is not spread over enough tiles)
+            # "tc": tcgen05 MMAs, 128 nodes per block; "warp": mma.sync, 32 nodes
+            # per warp; "auto": the tensor-core step from 2^20 interior nodes on
+            # (measured with the trained rate-form model, us per step, warp /
+            # tc: 256^2 10.3 / 14.4, 512^2 23.0 / 26.0, 768^2 45.8 / 46.0,
+            # 1024^2 75.2 / 73.3, 1536^2 162 / 152; on smaller grids a
+            # block's set-up is spread over too few tiles)
             self.closure_kernel = "auto"
         if model is not None and getattr(self, "_fallbacks", None) is None:
             self._fallbacks = runtime.DeviceBuffer(4)
@@ -626,7 +628,7 @@ class Simulation:
         if kernel not in ("auto", "tc", "warp"):
             raise ValueError(f"closure_kernel: {kernel!r} (auto, tc or warp)")
         if kernel == "auto":
-            return int(np.prod(self.domain.shape_in)) >= 1 << 18
+            return int(np.prod(self.domain.shape_in)) >= 1 << 20
         return kernel == "tc"
 
     def launches_per_step(self):
