@@ -807,21 +807,29 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
 #if LBM_Q <= 16 && (LBM_Q - LBM_NCONS) <= 8
   using namespace lbm_mlp;
   __shared__ __align__(16) __nv_bfloat16 w_s[BW2N];
-  __shared__ float b_s[2 * H + OUT];
+  __shared__ __align__(16) float b_s[2 * H + OUT];
   __shared__ __align__(16) __nv_bfloat16 x_s[kClosureWarps][32 * IN];
   __shared__ float y_s[kClosureWarps][kClosureWarpNodes * OUT];
   static_assert((BW2N * sizeof(__nv_bfloat16)) % 16 == 0, "weight block must be a whole number of 16-byte words");
+  static_assert(PB1 % 4 == 0 && PB2 % 4 == 0 && PB3 % 4 == 0 && H % 4 == 0 && OUT % 4 == 0, "16-byte bias chunks");
+  // weights and biases reach shared memory by cp.async while the warps pull
+  // their first nodes (both blocks 16-byte aligned, checked by the host);
+  // the block waits for them just before its first MLP evaluation
   {
-    const uint4* src = reinterpret_cast<const uint4*>(c.w);
-    uint4* dst = reinterpret_cast<uint4*>(w_s);
-    for (int i = threadIdx.x; i < (int)(BW2N * sizeof(__nv_bfloat16) / 16); i += blockDim.x) dst[i] = src[i];
+    const char* src = reinterpret_cast<const char*>(c.w);
+    char* dst = reinterpret_cast<char*>(w_s);
+    for (int i = threadIdx.x; i < (int)(BW2N * sizeof(__nv_bfloat16) / 16); i += blockDim.x)
+      lbm::cp_async16(dst + 16 * i, src + 16 * i);
+    char* bd = reinterpret_cast<char*>(b_s);
+    for (int i = threadIdx.x; i < (2 * H + OUT) / 4; i += blockDim.x) {
+      const float* bs = i < H / 4 ? c.params + PB1 + 4 * i
+                        : i < H / 2 ? c.params + PB2 + 4 * (i - H / 4)
+                                    : c.params + PB3 + 4 * (i - H / 2);
+      lbm::cp_async16(bd + 16 * i, bs);
+    }
+    lbm::cp_async_commit();
   }
-  for (int i = threadIdx.x; i < H; i += blockDim.x) {
-    b_s[i] = c.params[PB1 + i];
-    b_s[H + i] = c.params[PB2 + i];
-  }
-  for (int i = threadIdx.x; i < OUT; i += blockDim.x) b_s[2 * H + i] = c.params[PB3 + i];
-  __syncthreads();
+  bool staged = false;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   const Geo& g = a.g;
@@ -869,7 +877,13 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
         xr[k] = __float2bfloat16_rn(v);
       }
     }
-    __syncwarp();
+    if (!staged) {  // every block runs the same passes: a block-wide wait
+      lbm::cp_async_wait_all();
+      __syncthreads();
+      staged = true;
+    } else {
+      __syncwarp();
+    }
 #pragma unroll 1
     for (int t = 0; t < kClosureWarpNodes / 16; ++t) {
       const __nv_bfloat16* xt = &x_s[warp][t * 16 * IN];
@@ -919,6 +933,7 @@ __global__ void __launch_bounds__(32 * kClosureWarps, LBM_CLOSURE_MIN_BLOCKS) k_
     }
     __syncwarp();
   }
+  if (!staged) lbm::cp_async_wait_all();  // a block without nodes
 #endif
 }
 
@@ -1672,6 +1687,8 @@ static int closure_common(const void* f, void* fnew, const lbm_lattice* lat, con
     return lbm::fail(LBM_ERR_UNSUPPORTED, "%s: the closure MLP takes at most 16 moments and 8 corrections", who);
   if (!f || !fnew || f == fnew || (!tc && !wbf16) || !params || !norm)
     return lbm::fail(LBM_ERR_ARG, "%s: bad pointers", who);
+  if (!tc && (((uintptr_t)wbf16 | (uintptr_t)params) & 15u))
+    return lbm::fail(LBM_ERR_ARG, "%s: wbf16 and params must be 16-byte aligned", who);
   if (LBM_NPRM > 0 && !prm) return lbm::fail(LBM_ERR_ARG, "%s: %d parameters expected", who, LBM_NPRM);
   StepArgs a = make_step_args(*lat, prm);
   ClosureArgs c;

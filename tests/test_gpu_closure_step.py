@@ -101,8 +101,9 @@ def test_tensor_core_step_does_not_depend_on_blocks_per_sm():
 
 
 def test_auto_closure_kernel_follows_grid_size():
-    small = Simulation(W.shear_layer(n=64, nu=1e-3), dtype="float32")
-    large = Simulation(W.shear_layer(n=512, nu=1e-3), dtype="float32")
+    """auto: the warp-level step below 2^20 nodes, the tcgen05 step from there on."""
+    small = Simulation(W.shear_layer(n=768, nu=1e-3), dtype="float32")
+    large = Simulation(W.shear_layer(n=1024, nu=1e-3), dtype="float32")
     model = ClosureModel(init_params(1), _norm(scale_out=1e-4))
     for sim in (small, large):
         sim.set_closure(model)
