@@ -21,7 +21,6 @@ With N > 1 (torchrun) every rank runs an independent replica (the path has
 no cross-GPU exchange); value = total nodes updated by all ranks / max time.
 """
 import argparse
-import ctypes
 import json
 import os
 import subprocess

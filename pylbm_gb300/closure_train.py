@@ -48,14 +48,12 @@ parameters are kept.
 import argparse
 import json
 import math
-import os
 import time
 
 import numpy as np
 import sympy as sp
 import torch
 
-from . import runtime
 from .closure import IN, OUT, ClosureModel, _restrict, init_params, study_dicos
 from .scheme import Scheme
 
