@@ -46,3 +46,18 @@ def test_vorticity_matches_numpy():
     cons[0] += 3.0
     got = vorticity(torch.tensor(cons)[None])[0].numpy()
     assert np.allclose(got, np_vorticity(cons[1:], cons[0]), rtol=1e-14, atol=1e-14)
+
+
+def test_rate_bounds_keep_effective_rates_below_the_maximum():
+    from pylbm_gb300.closure_train import rate_bounds
+    rates = np.array([1.5, 1.5, 1.2, 1.2, 1.99489, 1.99489])
+    lo, hi = rate_bounds(rates, rate_max=1.9995)
+    assert np.all(lo[:6] <= 0.0) and np.all(hi[:6] >= 0.0) and np.all(lo <= hi) and np.all(lo >= -1.0)
+    assert np.all(rates * (1.0 + hi[:6]) <= 1.9995 + 1e-6)
+    assert np.all(rates * (1.0 + lo[:6]) > 0.0)
+    # the stresses (rates near 2) get the tighter lower bound; padding outputs are closed
+    assert np.all(lo[4:6] == np.float32(-0.02)) and np.all(lo[:4] == np.float32(-0.3))
+    assert np.all(lo[6:] == 0.0) and np.all(hi[6:] == 0.0)
+    # a rate already at the maximum cannot grow
+    lo2, hi2 = rate_bounds(np.array([1.9995]), rate_max=1.9995)
+    assert hi2[0] <= 1e-7

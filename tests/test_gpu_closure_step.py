@@ -170,3 +170,31 @@ def test_guard_keeps_the_plain_collision_for_a_broken_network(bad, kernel):
     b.run(12)
     assert np.array_equal(_moments(a), _moments(b))
     assert b.closure_fallbacks() == 12 * 64 * 64
+
+
+@pytest.mark.parametrize("kernel", ["tc", "warp"])
+def test_rate_form_bounds_a_broken_network(kernel):
+    """Rate form: NaN outputs trip the guard at every node (the run equals
+    the plain run bit for bit); absurdly large outputs only saturate lam_j at
+    its bounds, so the corrections stay within the relaxation's own change:
+    no node falls back and the run stays finite."""
+    from pylbm_gb300.closure_train import rate_bounds
+    d = W.shear_layer(n=64, nu=1e-3, seed=5)
+    plain = Simulation(d, dtype="float32")
+    plain.run(12)
+    for bad in ("nan", "huge"):
+        sim = Simulation(d, dtype="float32")
+        lo, hi = rate_bounds(sim.scheme.rates_numpy()[3:])
+        p = init_params(11).astype(np.float32)
+        p = np.full_like(p, np.nan) if bad == "nan" else p * 1e6
+        norm = _norm(scale_out=1.0)
+        sim.set_closure(ClosureModel(p, norm, rate=np.concatenate([lo, hi])))
+        sim.closure_kernel = kernel
+        sim.run(12)
+        if bad == "nan":
+            assert np.array_equal(_moments(plain), _moments(sim))
+            assert sim.closure_fallbacks() == 12 * 64 * 64
+        else:
+            assert sim.closure_fallbacks() == 0
+            assert np.all(np.isfinite(_moments(sim)))
+        sim.free()
