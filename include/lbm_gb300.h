@@ -411,9 +411,10 @@ int lbm_mlp_gradients(const void* x, const float* target, int32_t n, const void*
 int lbm_mlp_gradients_tc(const void* x, const float* target, int32_t n, const float* params, float* grad, float* loss,
                          void* stream);
 /* Vector-Jacobian product of the MLP on the same tensor-core kernel: adds
- * sum over samples of dy . dy_out/dparams to grad, for dy (n x 8 FP32, the
- * first 6 columns used) the gradient of some loss with respect to the
- * outputs lbm_mlp_forward_tc returns; *dot (device) receives sum dy . y.
+ * to grad the gradient with respect to params of sum over samples of dy . y,
+ * y the outputs lbm_mlp_forward_tc returns for x and dy (n x 8 FP32, the
+ * first 6 columns used) a given gradient of some loss with respect to y;
+ * *dot (device) receives sum dy . y.
  * This is the backward step of an MLP that sits inside a differentiated
  * computation (a training loss over several closure time steps); no
  * counterpart in pylbm, which has no learned closure (its relaxation is

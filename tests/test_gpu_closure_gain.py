@@ -2,7 +2,7 @@
 
 The model in pylbm_gb300/data was trained by pylbm_gb300.closure_train
 (rate form, truncated backpropagation along the closure run's own
-trajectory) on seeds 0..31 of the Re 30 000 double shear layer (1024^2
+trajectory) on seeds 0..199 of the Re 30 000 double shear layer (1024^2
 float64 runs restricted 4x); seed 100000 was not among them.  After 1500
 coarse steps the learned 256^2 run must be within 2 % (vorticity relative
 L2) of the float64 1024^2 solution, well below the plain 256^2 run and below
