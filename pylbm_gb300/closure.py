@@ -118,16 +118,18 @@ class Mlp:
         dy.free()
         return y.astype(np.float64)
 
-    def forward_device(self, x, n, y):
-        """lbm_mlp_forward_tc on device pointers: x (n, 16) BF16 rows, y (n, 8) FP32."""
+    def forward_device(self, x, n, y, stream=None):
+        """lbm_mlp_forward_tc on device pointers: x (n, 16) BF16 rows, y (n, 8)
+        FP32; on ``stream`` (a raw CUDA stream handle) if given, else the Mlp's."""
         runtime.check(self._core.lbm_mlp_forward_tc(ctypes.c_void_p(x), n, self.p.handle, ctypes.c_void_p(y),
-                                                    self.stream))
+                                                    self.stream if stream is None else stream))
 
-    def vjp_device(self, x, dy, n):
+    def vjp_device(self, x, dy, n, stream=None):
         """Adds the gradient of sum(dy . y) over the 6 used outputs to the
         gradient buffer (lbm_mlp_vjp_tc; device pointers, dy (n, 8) FP32)."""
         runtime.check(self._core.lbm_mlp_vjp_tc(ctypes.c_void_p(x), ctypes.c_void_p(dy), n, self.p.handle,
-                                                self.g.handle, self.loss.handle, self.stream))
+                                                self.g.handle, self.loss.handle,
+                                                self.stream if stream is None else stream))
 
     def vjp(self, x, dy):
         """(sum of dy . y, gradient float64) for host arrays x (n, 16), dy (n, 8)."""

@@ -46,6 +46,7 @@ parameters are kept.
     python -m pylbm_gb300.closure_train --out model.npz [--mode trajectory] [--form rate] [--seeds 24]
 """
 import argparse
+import ctypes
 import json
 import math
 import time
@@ -107,22 +108,29 @@ class CoarseStep:
         return self.populations(relaxed)
 
 
+def _torch_stream(device):
+    """PyTorch's current stream on ``device`` as a raw handle for the C ABI, so
+    the kernels are ordered with the tensor operations around them."""
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
 class _MlpOnKernels(torch.autograd.Function):
     """y = MLP(x) on lbm_mlp_forward_tc; backward accumulates the weight
-    gradient with lbm_mlp_vjp_tc into the Mlp's gradient buffer."""
+    gradient with lbm_mlp_vjp_tc into the Mlp's gradient buffer (both on
+    PyTorch's current stream)."""
 
     @staticmethod
     def forward(ctx, anchor, x, mlp):
         n = x.shape[0]
         y = torch.empty((n, OUT), dtype=torch.float32, device=x.device)
-        mlp.forward_device(x.data_ptr(), n, y.data_ptr())
+        mlp.forward_device(x.data_ptr(), n, y.data_ptr(), stream=_torch_stream(x.device))
         ctx.mlp, ctx.x = mlp, x
         return y
 
     @staticmethod
     def backward(ctx, gy):
         gy = gy.contiguous().to(torch.float32)
-        ctx.mlp.vjp_device(ctx.x.data_ptr(), gy.data_ptr(), ctx.x.shape[0])
+        ctx.mlp.vjp_device(ctx.x.data_ptr(), gy.data_ptr(), ctx.x.shape[0], stream=_torch_stream(gy.device))
         return torch.zeros(1, device=gy.device), None, None
 
 
@@ -297,6 +305,7 @@ def train_on_trajectories(model, inits, refs, every, segment=16, episodes=8, bat
     step = CoarseStep(scheme or Scheme(study_dicos(0, inits.shape[-1])), device=device)
     closure = KernelClosure(model, device)
     mlp = model.mlp
+    saved_stream, mlp.stream = mlp.stream, _torch_stream(device)  # Adam and copies ordered with the tensors
     gen = torch.Generator(device="cpu").manual_seed(seed)
     t_end = refs.shape[1] * every
     nseg = t_end // segment
@@ -335,6 +344,7 @@ def train_on_trajectories(model, inits, refs, every, segment=16, episodes=8, bat
             losses.append(float(loss.detach()))
         rec = {"episode": ep + 1, "loss_first": losses[0], "loss_last": losses[-1], "loss_mean": float(np.mean(losses))}
         if rollout is not None:
+            torch.cuda.synchronize()  # the last Adam step landed before the runs read the weights
             errs = rollout(model)
             rec["rollout"] = errs
             if float(np.mean(errs)) < best[0]:
@@ -345,6 +355,7 @@ def train_on_trajectories(model, inits, refs, every, segment=16, episodes=8, bat
     if best[1] is not None:
         mlp.set_params(best[1])
         history.append({"kept_rollout_mean": best[0]})
+    mlp.stream = saved_stream
     return history
 
 
@@ -386,6 +397,7 @@ def train_aposteriori(model, starts, targets, iters=1500, batch=4, lr=3e-4, clip
     step = CoarseStep(scheme or Scheme(study_dicos(0, starts.shape[-1])), device=device)
     closure = KernelClosure(model, device)
     mlp = model.mlp
+    saved_stream, mlp.stream = mlp.stream, _torch_stream(device)  # Adam and copies ordered with the tensors
     gen = torch.Generator(device="cpu").manual_seed(seed)
     history = []
     mlp.g.zero(mlp.stream)
@@ -417,6 +429,7 @@ def train_aposteriori(model, starts, targets, iters=1500, batch=4, lr=3e-4, clip
             if val is not None:
                 rec["val"] = validation(step, closure, *val)
             if rollout is not None:
+                torch.cuda.synchronize()  # the last Adam step landed before the runs read the weights
                 errs = rollout(model)
                 rec["rollout"] = errs
                 if float(np.mean(errs)) < best[0]:
@@ -428,6 +441,7 @@ def train_aposteriori(model, starts, targets, iters=1500, batch=4, lr=3e-4, clip
     if best[1] is not None:
         mlp.set_params(best[1])
         history.append({"kept_rollout_mean": best[0]})
+    mlp.stream = saved_stream
     return history
 
 

@@ -96,3 +96,24 @@ def test_unrolled_training_reduces_the_segment_loss():
     train_aposteriori(model, start, targets, iters=60, batch=1, lr=3e-3, report_every=1000, scheme=sim.scheme)
     after = float(segment_loss(coarse, KernelClosure(model, "cuda"), start, targets))
     assert after < 0.8 * before, (before, after)
+
+
+def test_training_along_own_trajectories_runs_and_moves_the_rate_model():
+    """train_on_trajectories on a small case (coarse 32^2 from 64^2 float64
+    runs, 48 steps, 8-step segments): every segment's loss is finite, the
+    parameters move, and the rate-form model stays a valid closure."""
+    from pylbm_gb300.closure_train import rate_model, reference_trajectories, train_on_trajectories
+    inits, refs = reference_trajectories([3, 4], t_end=48, every=4, n_fine=64, factor=2, re=3000.0)
+    assert inits.shape == (2, 9, 32, 32) and refs.shape == (2, 12, 3, 32, 32)
+    scheme = Simulation(study_dicos(3, 32, re=3000.0), dtype="float32").scheme
+    step = CoarseStep(scheme, device="cuda")
+    model = rate_model(step, inits)
+    p0 = model.mlp.params_host()
+    hist = train_on_trajectories(model, inits, refs, every=4, segment=8, episodes=3, batch=2, lr=1e-3,
+                                 scheme=scheme)
+    assert len(hist) == 3 and all(np.isfinite(h["loss_mean"]) for h in hist)
+    assert np.abs(model.mlp.params_host() - p0).max() > 0
+    sim = Simulation(study_dicos(3, 32, re=3000.0), dtype="float32")
+    sim.set_closure(model)
+    sim.run(20)
+    assert sim.closure_fallbacks() == 0 and np.all(np.isfinite(sim.m[1]))
