@@ -61,3 +61,67 @@ def test_rate_bounds_keep_effective_rates_below_the_maximum():
     # a rate already at the maximum cannot grow
     lo2, hi2 = rate_bounds(np.array([1.9995]), rate_max=1.9995)
     assert hi2[0] <= 1e-7
+
+
+def _closure_case(form, seed=3, scale=0.5):
+    import mlp_oracle as mo
+    from pylbm_gb300.closure_train import rate_bounds
+    o = OracleSimulation(study_dicos(seed, 16, re=3000.0))
+    o.initialize()
+    params = mo.init_params(seed) * scale
+    norm = np.zeros(48)
+    norm[:9] = [1.0, 0, 0, -2.0, 1.0, 0, 0, 0, 0]
+    norm[16:25] = [10.0, 20.0, 20.0, 10.0, 10.0, 20.0, 20.0, 50.0, 50.0]
+    rate = None
+    if form == "rate":
+        lo, hi = rate_bounds(o.scheme.rates_numpy()[3:])
+        rate = np.concatenate([lo, hi]).astype(np.float64)
+        norm[40:46] = 1.0
+    else:
+        norm[40:46] = 1e-4
+    return o, params, norm, rate
+
+
+@pytest.mark.parametrize("form", ["additive", "rate"])
+def test_closure_oracle_matches_the_training_restatement(form):
+    """The oracle's fused closure step and the PyTorch restatement (float64,
+    same network through the MLP oracle) agree; corrections leave rho and q."""
+    import mlp_oracle as mo
+    from closure_oracle import closure_step
+    o, params, norm, rate = _closure_case(form)
+    f0 = _interior(o)
+    ref, fallbacks = closure_step(f0, o.scheme, params, norm, rate=rate)
+    assert fallbacks == 0
+
+    def closure(m, relaxed):
+        b, nv, n0, n1 = m.shape
+        rows = m[0].reshape(nv, -1).T.numpy()
+        x = np.zeros((rows.shape[0], mo.IN))
+        x[:, :nv] = (rows - norm[:nv]) * norm[16:16 + nv]
+        y, _ = mo.forward(params, x)
+        z = y[:, :6] * norm[40:46] + norm[32:38]
+        if rate is None:
+            corr = z
+        else:
+            lam = rate[:6] + (rate[8:14] - rate[:6]) / (1.0 + np.exp(-z))
+            corr = lam * (relaxed - m)[0, 3:].reshape(6, -1).T.numpy()
+        return torch.tensor(corr.T.reshape(1, 6, n0, n1))
+
+    step = CoarseStep(o.scheme, dtype=torch.float64)
+    got = step(torch.tensor(f0)[None], closure)[0].numpy()
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+    plain = step(torch.tensor(f0)[None])[0].numpy()
+    m_ref = np.einsum("ij,j...->i...", o.scheme.M, ref)
+    m_plain = np.einsum("ij,j...->i...", o.scheme.M, plain)
+    assert np.abs(m_ref[:3] - m_plain[:3]).max() < 1e-14
+    assert np.abs(m_ref[3:] - m_plain[3:]).max() > 1e-8  # the network changed the step
+
+
+def test_closure_oracle_guard_keeps_the_plain_collision():
+    from closure_oracle import closure_step
+    o, params, norm, rate = _closure_case("additive")
+    f0 = _interior(o)
+    plain, _ = closure_step(f0, o.scheme, np.zeros_like(params), norm)
+    bad, fallbacks = closure_step(f0, o.scheme, np.full_like(params, np.nan), norm, guard=(8.0, 1e-3))
+    assert fallbacks == f0[0].size
+    assert np.array_equal(bad, plain)

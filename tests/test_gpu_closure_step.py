@@ -198,3 +198,48 @@ def test_rate_form_bounds_a_broken_network(kernel):
             assert sim.closure_fallbacks() == 0
             assert np.all(np.isfinite(_moments(sim)))
         sim.free()
+
+
+@pytest.mark.parametrize("form", ["additive", "rate"])
+@pytest.mark.parametrize("kernel", ["tc", "warp"])
+def test_closure_step_against_the_oracle(form, kernel):
+    """Five fused closure steps (FP32 storage and arithmetic, BF16 network,
+    both output forms) against the float64 CPU oracle of the same step
+    (oracle/closure_oracle.py): the two differ by far less than the closure
+    changes the flow, and conserve the same mass and momentum."""
+    from closure_oracle import closure_step
+    from pylbm_gb300.closure_train import rate_bounds
+    d = W.shear_layer(n=48, nu=1e-3, seed=4)
+    sim = Simulation(d, dtype="float32")
+    plain = Simulation(d, dtype="float32")
+    f = np.array([sim.F[k] for k in range(sim.scheme.nv)])
+    p = (init_params(3) * 0.5).astype(np.float32)
+    if form == "rate":
+        lo, hi = rate_bounds(sim.scheme.rates_numpy()[3:])
+        model = ClosureModel(p, _norm(scale_out=1.0), rate=np.concatenate([lo, hi]))
+    else:
+        model = ClosureModel(p, _norm(scale_out=1e-4))
+    sim.set_closure(model)
+    sim.closure_kernel = kernel
+    steps = 5
+    sim.run(steps)
+    plain.run(steps)
+    total = 0
+    for _ in range(steps):
+        f, fb = closure_step(f, sim.scheme, model.mlp.params_host().astype(np.float64), model.norm,
+                             rate=model.rate, guard=model.guard)
+        total += fb
+    m_ref = np.einsum("ij,j...->i...", sim.scheme.M, f)
+    got = np.array([sim.m[k] for k in range(sim.scheme.nv)])
+    base = np.array([plain.m[k] for k in range(sim.scheme.nv)])
+    effect = np.abs(m_ref[1:3] - base[1:3]).max()
+    diff = np.abs(got[1:3] - m_ref[1:3]).max()
+    assert total == 0 and sim.closure_fallbacks() == 0
+    assert effect > 1e-7
+    # the oracle accumulates each layer in float64, the kernels in FP32 in
+    # their own order: a hidden activation can round to the neighbouring BF16
+    # value (up to 5e-3 of the output scale, tests/test_gpu_closure.py), so
+    # node corrections differ by a few per mille; a wrong formula would differ
+    # by the whole effect
+    assert diff < 1e-1 * effect, (diff, effect)
+    assert np.abs(got[0] - m_ref[0]).max() < 1e-6
