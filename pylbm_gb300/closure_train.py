@@ -278,6 +278,8 @@ def reference_trajectories(seeds, t_end, every, n_fine=1024, factor=4, re=30000.
 
 
 def _snapshot_error(step, f, ref):
+    """Relative squared vorticity error plus relative squared momentum error
+    of the populations ``f`` against the conserved moments ``ref``, batch mean."""
     cons = step.moments(f)[:, :3]
     ref = ref.to(step.dtype)
     w, w_ref = vorticity(cons), vorticity(ref)
@@ -367,12 +369,7 @@ def segment_loss(step, closure, f0, targets):
     unroll = targets.shape[1]
     for k in range(unroll):
         f = step(f, closure)
-        cons = step.moments(f)[:, :3]
-        ref = targets[:, k].to(step.dtype)
-        w, w_ref = vorticity(cons), vorticity(ref)
-        ew = ((w - w_ref) ** 2).sum(dim=(1, 2)) / (w_ref ** 2).sum(dim=(1, 2))
-        eq = ((cons[:, 1:] - ref[:, 1:]) ** 2).sum(dim=(1, 2, 3)) / (ref[:, 1:] ** 2).sum(dim=(1, 2, 3))
-        total = total + (ew + eq).mean()
+        total = total + _snapshot_error(step, f, targets[:, k])
     return total / unroll
 
 
