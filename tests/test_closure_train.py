@@ -125,3 +125,26 @@ def test_closure_oracle_guard_keeps_the_plain_collision():
     bad, fallbacks = closure_step(f0, o.scheme, np.full_like(params, np.nan), norm, guard=(8.0, 1e-3))
     assert fallbacks == f0[0].size
     assert np.array_equal(bad, plain)
+
+
+def test_shipped_closure_model_is_a_bounded_rate_model():
+    """The model in pylbm_gb300/data: rate form, every effective rate of the
+    study's coarse scheme at most 1.9995, finite parameters, and the study
+    record beside it holds 20 held-out seeds with the learned run better than
+    the plain one on each."""
+    import json
+    import os
+    from pylbm_gb300.closure_study import DEFAULT_MODEL
+    from pylbm_gb300.scheme import Scheme
+    d = np.load(DEFAULT_MODEL, allow_pickle=False)
+    assert d["params"].size == 5768 and np.all(np.isfinite(d["params"]))
+    assert d["norm"].size == 48 and "rate" in d.files
+    rate = d["rate"]
+    rates = Scheme(study_dicos(0, 256)).rates_numpy()[3:]
+    assert np.all(rate[:8] <= rate[8:]) and np.all(rate[:8] >= -1.0)
+    assert np.all(rates * (1.0 + rate[8:14]) <= 1.9995 + 1e-6) and np.all(rates * (1.0 + rate[:6]) > 0.0)
+    study = json.load(open(os.path.join(os.path.dirname(DEFAULT_MODEL), "closure_d2q9_shear_re30000_study.json")))
+    rows = study["rows"]
+    assert len(rows) == 20 and all(r["seed"] >= 100000 for r in rows)
+    assert all(r["learned_256"]["vort_rel_l2"] < r["plain_256"]["vort_rel_l2"] for r in rows)
+    assert all(r["learned_256"]["vort_rel_l2"] < 0.02 for r in rows)
