@@ -3,10 +3,14 @@ non-conserved moments of a coarse simulation.
 
 ``Mlp`` owns the FP32 master parameters, their BF16 copies, the Adam moments
 and the gradient buffer on the device, and drives the tensor-core kernels of
-liblbm_gb300.so (lbm_mlp_forward / lbm_mlp_gradients / lbm_mlp_adam).  The
-inputs are the node's pre-collision moments (normalised), the outputs the
-corrections of the non-conserved moments (normalised); conserved moments are
-never touched, so mass and momentum stay exactly conserved.
+liblbm_gb300.so (lbm_mlp_forward(_tc) / lbm_mlp_gradients(_tc) /
+lbm_mlp_vjp_tc / lbm_mlp_adam).  The inputs are the node's pre-collision
+moments (normalised), the outputs the corrections of the non-conserved
+moments (additive form) or the factors of their relaxation rates (rate
+form); conserved moments are never touched, so mass and momentum stay
+exactly conserved.  The first, one-step training of this module
+(generate_training_data / train) is kept beside the a-posteriori training
+of closure_train.py, which produced the shipped model.
 """
 import ctypes
 
